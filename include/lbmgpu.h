@@ -1,0 +1,230 @@
+/*
+ * lbmgpu.h -- C ABI of the GB300 forward/adjoint lattice-Boltzmann library.
+ *
+ * One opaque handle owns one lattice (its populations, design field gamma,
+ * adjoint populations, FP64 sensitivity field and checkpoint slots) resident
+ * in device memory.  A handle is single-threaded, like one PETSc rank of the
+ * reference.  Every entry point returns an int status: LBM_OK (0) on
+ * success, a negative LBM_ERR_* code otherwise; lbm_last_error() gives the
+ * text.  Host arrays crossing this boundary are FP64 in the reference's
+ * DMDA order: cell index c = (z*ny + y)*nx + x (x fastest) and, for
+ * per-cell vectors, AoS element c*Q + q with the reference's lattice
+ * numbering (D2Q9 / D3Q19 / D2Q5 of latticeBoltzmann/lattices{2,3}d.hh).
+ *
+ * Time-step convention (the reference applications' driver loop, e.g.
+ * applications/RobustPump2d/robustPump2d.cc:234-249):
+ *   f_0 = feq(initial macros)                       (initializeAtEquilibrium)
+ *   f_{t+1} = BC_{t+1}( stream( collide(f_t) ) )     (collide(); stream())
+ *   J = sum_{t=1..N} F(macros(f_t))                  (computeMacroFunctional)
+ * and the reverse sweep for t = N..1 (robustPump2d.cc:268-276):
+ *   adjointCollide(f_t); computeCollideSource(f_t); adjointStream().
+ * The "state" a handle holds is f_t: post-stream, post-boundary,
+ * pre-collision populations.
+ */
+#ifndef LBMGPU_H
+#define LBMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBMGPU_ABI_VERSION 1
+#define LBM_MAX_BC 8
+
+/* Status codes.  PETSc's PetscErrorCode is 0 = ok; the reference's
+ * "unsupported" case (PETSC_ERR_SUP, boundaryConditions/LBBoundaryLoop.cc:32-38)
+ * maps to LBM_ERR_SUP. */
+#define LBM_OK             0
+#define LBM_ERR_ARG       -1  /* bad argument: null pointer, bad size, bad box */
+#define LBM_ERR_SUP       -2  /* combination not supported */
+#define LBM_ERR_CUDA      -3  /* CUDA runtime error, or no CUDA device */
+#define LBM_ERR_MEM       -4  /* device or host allocation failed */
+#define LBM_ERR_STATE     -5  /* call out of order (e.g. no design set) */
+#define LBM_ERR_NONFINITE -6  /* NaN/Inf detected in inputs or results */
+
+/* Lattices (latticeBoltzmann/lattices2d.hh:16-62, lattices3d.hh:141-160). */
+#define LBM_D2Q9        0
+#define LBM_D3Q19       1
+#define LBM_D2Q9_D2Q5   2   /* flow D2Q9 + temperature D2Q5 (double distribution) */
+
+/* Collision operators of the flow lattice. */
+#define LBM_BGK 0   /* IncompressibleBGK2d (dynamics/incompressibleBGK2d.hh:94-153) */
+#define LBM_MRT 1   /* IncompressibleMRT2d / IncompressibleMRT3d (dynamics/MRT3d.hh:28-200) */
+
+/* Population storage in device memory.  Compute precision is FP64 for
+ * LBM_STORE_FP64 and FP32 for the two shifted forms, which store the
+ * deviation f_i - w_i. */
+#define LBM_STORE_FP64 0
+#define LBM_STORE_FP32 1
+#define LBM_STORE_FP16 2
+
+/* Boundary condition kinds (applied after streaming on the boundary box). */
+#define LBM_BC_VELOCITY    1  /* Zou-He (2D, ZouHe2d.hh:23-56) / Hecht (3D, Hecht3d.hh:62-94) */
+#define LBM_BC_PRESSURE    2  /* Zou-He (ZouHe2d.hh:245-281) / Hecht (Hecht3d.hh:175-209) */
+#define LBM_BC_TEMPERATURE 3  /* thermal Zou-He Dirichlet (thermalZouHe2d.hh:63-97) */
+#define LBM_BC_THERMAL_NEUMANN 4 /* zero-gradient outflow of the temperature lattice */
+
+/* Faces.  West = x min, East = x max, South = y min, North = y max,
+ * Bottom = z min, Top = z max. */
+#define LBM_FACE_WEST   0
+#define LBM_FACE_EAST   1
+#define LBM_FACE_SOUTH  2
+#define LBM_FACE_NORTH  3
+
+/* Inflow profiles.  value(t) = value * (1 + amp*sin(2*pi*t/period)). */
+#define LBM_PROFILE_UNIFORM   0
+#define LBM_PROFILE_PARABOLIC 1  /* 2D: (m^2-(y-m)^2)/m^2, m=(ny-1)/2 (applications/diffuser/diffuser.cc:22-31);
+                                    3D: product of the y and z parabolas */
+
+/* Objectives (functionals/LBMacroFunctional.hh:6-14). */
+#define LBM_OBJ_NONE          0
+#define LBM_OBJ_PRESSURE_DROP 1  /* functionals/pressureDrop2d.hh:9-70 */
+#define LBM_OBJ_DISSIPATION   2  /* porous + viscous dissipated power (no reference counterpart) */
+#define LBM_OBJ_HEAT_FLUX     3  /* functionals/temperatureFlow2d.hh:10-63 */
+
+typedef struct lbm_bc {
+  int kind;        /* LBM_BC_* */
+  int face;        /* LBM_FACE_* */
+  int profile;     /* LBM_PROFILE_* (velocity only) */
+  int box[6];      /* x0,x1,y0,y1,z0,z1 inclusive; z0=z1=0 in 2D */
+  double value;    /* u_max (velocity), rho0 (pressure), T (temperature) */
+  double amp;      /* relative oscillation amplitude, 0 = steady */
+  double period;   /* oscillation period in time steps */
+} lbm_bc;
+
+typedef struct lbm_config {
+  int lattice;     /* LBM_D2Q9, LBM_D3Q19, LBM_D2Q9_D2Q5 */
+  int collision;   /* LBM_BGK, LBM_MRT */
+  int storage;     /* LBM_STORE_* */
+  int nx, ny, nz;  /* nz = 1 in 2D */
+  double omega;    /* shear relaxation rate 1/tau */
+  /* MRT rates.  D3Q19: s1,s2,s4,s10,s16,we,wej,wxx (MRT3d.hh:9-22);
+   * D2Q9: s1 (energy), s2 (eps), s46 (heat flux) (incompressibleMRT2d.hh:88-90). */
+  double mrt[8];
+  /* Partial bounce-back (dynamics/partialBouncebackCollision.hh:53-65):
+   * mixing factor = 0.5 * interp_scale * BP_q(gamma),
+   * BP_q(s) = 1 - s(1+q)/(q+s) (core/interpolationFunctions.hh:17-21).
+   * interp_scale = 1 is the reference's plain BPInterpolation;
+   * interp_scale = 2*alpha_max gives alpha(gamma) = alpha_max*q(1-gamma)/(q+gamma). */
+  double interp_scale;
+  double interp_q;
+  /* Temperature lattice (LBM_D2Q9_D2Q5 only): omega_T(gamma) =
+   * 1/(3*diffusivity*RAMP(gamma) + 0.5) (dynamics/thermalObstacleCollision.hh:47-53),
+   * RAMP(s) = (s(Ck(1+q)-1)+1)/(Ck(1+q s)) (interpolationFunctions.hh:37-49).
+   * Heating of the solid: g_i += (1-gamma) w_i heat_rate (heat_T - T). */
+  double diffusivity;
+  double ramp_q, ramp_ck;
+  double heat_rate, heat_T;
+  int nbc;
+  lbm_bc bc[LBM_MAX_BC];
+  int objective;       /* LBM_OBJ_* */
+  int obj_in[6];       /* inflow box of the pressure drop */
+  int obj_out[6];      /* outflow box (pressure drop, heat flux) */
+  double obj_weight;   /* timeConst: weight of each step's value (1/N for a time average) */
+} lbm_config;
+
+typedef struct lbm_handle lbm_handle;
+
+typedef struct lbm_gradient_stats {
+  int64_t forward_steps;     /* forward steps of the first sweep */
+  int64_t recomputed_steps;  /* forward steps re-run by the checkpoint schedule */
+  int64_t adjoint_steps;
+  double forward_ms, reverse_ms;  /* device time of the two sweeps (CUDA events) */
+} lbm_gradient_stats;
+
+/* Fill a config with the reference defaults: D2Q9 BGK FP64, omega 1,
+ * MRT3d_Compile_constants, plain BP (scale 1, q 1), no BCs, no objective. */
+void lbm_config_default(lbm_config* cfg);
+
+/* Validate the config and allocate device memory.  Replaces
+ * IsothermalLBSolver2d<Op>::make (latticeBoltzmann/isothermalLBSolver2d.hh:20-60)
+ * plus addBoundaryCondition, and the adjoint set-up of makeSourceAdjoint
+ * (isothermalLBSolver2d.hh:62-110). */
+int lbm_create(const lbm_config* cfg, lbm_handle** out);
+int lbm_destroy(lbm_handle* h);
+
+/* Text of the last error of h (or of the last failed lbm_create if h is NULL). */
+const char* lbm_last_error(const lbm_handle* h);
+
+/* Cells (nx*ny*nz) and populations per cell (9, 19 or 9+5). */
+int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop);
+
+/* Design field gamma in [0,1], one double per cell.  Replaces
+ * LBSolver::setFieldFromDesignVec (latticeBoltzmann/LBSolver.cc:333-348). */
+int lbm_set_design(lbm_handle* h, const double* gamma);
+
+/* f_0 = feq(macros) and t = 0.  macros: NULL for rho=1, u=0 (T=0), else
+ * per cell {rho,ux,uy} (D2Q9), {rho,ux,uy,uz} (D3Q19) or {rho,ux,uy,T}.
+ * Replaces LBSolver::initializeAtEquilibrium (LBSolver.cc:234-249). */
+int lbm_init_equilibrium(lbm_handle* h, const double* macros);
+
+/* Advance the state nsteps time steps from t0 to t0+nsteps; accumulate the
+ * objective of each new state: J_steps[k] = weight*F(f_{t0+1+k}).
+ * J_steps and J_sum may be NULL.  Replaces the app loop around
+ * LBSolver::collide/stream (LBSolver.cc:163-206) and
+ * LBSolver::computeMacroFunctional (LBSolver.cc:74-91). */
+int lbm_forward(lbm_handle* h, int nsteps, double* J_steps, double* J_sum);
+
+/* Current time step t of the state. */
+int lbm_get_time(const lbm_handle* h, int* t);
+
+/* Populations of the state f_t, FP64 AoS (post-stream, post-BC). */
+int lbm_get_populations(const lbm_handle* h, double* f);
+/* Replace the state by host populations f (FP64 AoS) at time step t.
+ * Replaces LBSolver::setDistributions + setCurrentTimestep (LBSolver.cc:65-97). */
+int lbm_set_populations(lbm_handle* h, const double* f, int t);
+/* Macros of the state f_t: {rho,ux,uy}, {rho,ux,uy,uz} or {rho,ux,uy,T}. */
+int lbm_get_macros(const lbm_handle* h, double* mac);
+
+/* Zero the adjoint populations and the sensitivity field.
+ * Replaces AdjointLBSolver::resetAdjoints (adjointLBSolver.cc:138-145). */
+int lbm_adjoint_reset(lbm_handle* h);
+
+/* One reverse time step for the forward state currently held (f_t, t >= 1):
+ * adjoint collision at f_t with sensitivity accumulation, objective source
+ * weight*dF/df_t, adjoint boundary conditions at t, adjoint stream.
+ * Replaces AdjointLBSolver::adjointCollide + computeCollideSource +
+ * computeSensitivitySource + adjointStream (adjointLBSolver.cc:28-122). */
+int lbm_adjoint_step(lbm_handle* h);
+
+/* Adjoint populations (FP64 AoS) of the post-collision state of the step
+ * below the last reverse step, i.e. what adjointGlobal holds after
+ * AdjointLBSolver::adjointStream. */
+int lbm_get_adjoint(const lbm_handle* h, double* lam);
+
+/* dJ/dgamma accumulated so far, one double per cell.
+ * Replaces AdjointLBSolver::getSensitivities (adjointLBSolver.cc:153-157). */
+int lbm_get_sensitivity(const lbm_handle* h, double* sens);
+
+/* Full gradient: f_0 from uniform rest (or the macros of the last
+ * lbm_init_equilibrium), nsteps forward steps with Wang et al. dynamic
+ * checkpointing in nsnapshots device slots, then the reverse sweep.
+ * Replaces the checkpointed driver of robustPump2d.cc:234-276 with
+ * LBDynamicCheckpointing (topOpt/LBCheckpointing.cc:322-351,
+ * topOpt/dynamicCheckpointing.cc:9-54, topOpt/WangCheckpointing.cc:36-126).
+ * J (may be NULL) gets sum_t weight*F(f_t); dJdgamma (may be NULL) gets
+ * the sensitivity field; stats may be NULL. */
+int lbm_gradient(lbm_handle* h, int nsteps, int nsnapshots, double* J,
+                 double* dJdgamma, lbm_gradient_stats* stats);
+
+/* Device-time measurement for benchmarks: run `nsteps` forward steps
+ * (which = 0) or reverse steps over the current state (which = 1; the
+ * forward state is left unchanged) on the handle's stream, bracketed by
+ * CUDA events recorded on that stream.  *ms gets the elapsed time. */
+int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms);
+
+/* Number of kernel launches issued by this handle since creation. */
+int lbm_get_launch_count(const lbm_handle* h, int64_t* launches);
+
+/* Wang et al. checkpoint schedule on the host only: forward-recompute
+ * steps needed to reverse nsteps steps with nsnapshots slots
+ * (WangCheckpointing.cc:72-162 with DynamicCheckpointing.cc:9-54). */
+int lbm_wang_recompute_count(int nsteps, int nsnapshots, int64_t* recomputed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBMGPU_H */

@@ -1,0 +1,382 @@
+"""Python host mirror of the GB300 LBM library's C ABI (include/lbmgpu.h).
+
+The classes below keep the reference's C++ surface so that driver code reads
+like the reference applications:
+
+* ``IsothermalLBSolver`` -- ``IsothermalLBSolver2d/3d<Op>`` plus the parts of
+  ``LBSolver`` a driver calls (latticeBoltzmann/LBSolver.hh:14-73,
+  isothermalLBSolver2d.hh:20-110): ``setFieldFromDesignVec``,
+  ``initializeAtEquilibrium``, ``collideAndStream``, ``computeMacroFunctional``,
+  ``getDistributions`` / ``setDistributions``.
+* ``AdjointLBSolver`` -- adjointLatticeBoltzmann/adjointLBSolver.hh:11-46:
+  ``resetAdjoints``, ``adjointStep`` (adjointCollide + computeCollideSource +
+  adjointStream), ``getSensitivities``.
+* ``LBDynamicCheckpointing`` -- the Wang et al. checkpointed gradient
+  (topOpt/LBCheckpointing.hh:20-29) run inside the library with device slots.
+
+All work happens in the compiled CUDA library ``liblbmgpu.so``; this module only
+marshals arguments.  There is no CPU fallback: if the library is missing the
+import of the solver classes raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbmgpu.so")
+
+# lattices, operators, storage, boundaries, objectives (include/lbmgpu.h)
+D2Q9, D3Q19, D2Q9_D2Q5 = 0, 1, 2
+BGK, MRT = 0, 1
+STORE_FP64, STORE_FP32, STORE_FP16 = 0, 1, 2
+BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE, BC_THERMAL_NEUMANN = 1, 2, 3, 4
+FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
+PROFILE_UNIFORM, PROFILE_PARABOLIC = 0, 1
+OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX = 0, 1, 2, 3
+MAX_BC = 8
+
+STATUS_TEXT = {0: "ok", -1: "bad argument", -2: "unsupported", -3: "CUDA error",
+               -4: "out of memory", -5: "call out of order", -6: "non-finite value"}
+
+# MRT rates: d'Humieres defaults (dynamics/MRT3d.hh:9-22) and the 2D ones
+# (dynamics/incompressibleMRT2d.hh:88-90)
+MRT3D_DEFAULT = (1.19, 1.4, 1.2, 1.4, 1.4, 3.0, -5.5, -0.5)
+MRT2D_DEFAULT = (1.4, 1.4, 1.2, 0.0, 0.0, 0.0, 0.0, 0.0)
+
+
+class CBC(C.Structure):
+    _fields_ = [("kind", C.c_int), ("face", C.c_int), ("profile", C.c_int),
+                ("box", C.c_int * 6), ("value", C.c_double), ("amp", C.c_double),
+                ("period", C.c_double)]
+
+
+class CConfig(C.Structure):
+    _fields_ = [("lattice", C.c_int), ("collision", C.c_int), ("storage", C.c_int),
+                ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("omega", C.c_double), ("mrt", C.c_double * 8),
+                ("interp_scale", C.c_double), ("interp_q", C.c_double),
+                ("diffusivity", C.c_double), ("ramp_q", C.c_double), ("ramp_ck", C.c_double),
+                ("heat_rate", C.c_double), ("heat_T", C.c_double),
+                ("nbc", C.c_int), ("bc", CBC * MAX_BC),
+                ("objective", C.c_int), ("obj_in", C.c_int * 6), ("obj_out", C.c_int * 6),
+                ("obj_weight", C.c_double)]
+
+
+class CGradStats(C.Structure):
+    _fields_ = [("forward_steps", C.c_int64), ("recomputed_steps", C.c_int64),
+                ("adjoint_steps", C.c_int64), ("forward_ms", C.c_double),
+                ("reverse_ms", C.c_double)]
+
+
+@dataclass
+class Boundary:
+    kind: int
+    face: int
+    box: Sequence[int]
+    value: float
+    profile: int = PROFILE_UNIFORM
+    amp: float = 0.0
+    period: float = 1.0
+
+
+@dataclass
+class Config:
+    """Python view of ``lbm_config``; ``to_c()`` gives the C struct."""
+    lattice: int = D2Q9
+    collision: int = BGK
+    storage: int = STORE_FP64
+    nx: int = 1
+    ny: int = 1
+    nz: int = 1
+    omega: float = 1.0
+    mrt: Sequence[float] = MRT3D_DEFAULT
+    interp_scale: float = 1.0
+    interp_q: float = 1.0
+    diffusivity: float = 0.0
+    ramp_q: float = 1.0
+    ramp_ck: float = 1.0
+    heat_rate: float = 0.0
+    heat_T: float = 1.0
+    bcs: List[Boundary] = field(default_factory=list)
+    objective: int = OBJ_NONE
+    obj_in: Sequence[int] = (0, 0, 0, 0, 0, 0)
+    obj_out: Sequence[int] = (0, 0, 0, 0, 0, 0)
+    obj_weight: float = 1.0
+
+    @property
+    def ncells(self) -> int:
+        return self.nx * self.ny * (self.nz if self.lattice == D3Q19 else 1)
+
+    @property
+    def npop(self) -> int:
+        return {D2Q9: 9, D3Q19: 19, D2Q9_D2Q5: 14}[self.lattice]
+
+    @property
+    def nmac(self) -> int:
+        return {D2Q9: 3, D3Q19: 4, D2Q9_D2Q5: 4}[self.lattice]
+
+    def replace(self, **kw) -> "Config":
+        d = dict(self.__dict__)
+        d["bcs"] = list(self.bcs)
+        d.update(kw)
+        return Config(**d)
+
+    def to_c(self) -> CConfig:
+        if len(self.bcs) > MAX_BC:
+            raise ValueError("at most %d boundary conditions" % MAX_BC)
+        c = CConfig()
+        c.lattice, c.collision, c.storage = self.lattice, self.collision, self.storage
+        c.nx, c.ny, c.nz = self.nx, self.ny, (self.nz if self.lattice == D3Q19 else 1)
+        c.omega = self.omega
+        for i, v in enumerate(list(self.mrt)[:8]):
+            c.mrt[i] = v
+        c.interp_scale, c.interp_q = self.interp_scale, self.interp_q
+        c.diffusivity, c.ramp_q, c.ramp_ck = self.diffusivity, self.ramp_q, self.ramp_ck
+        c.heat_rate, c.heat_T = self.heat_rate, self.heat_T
+        c.nbc = len(self.bcs)
+        for k, b in enumerate(self.bcs):
+            cb = c.bc[k]
+            cb.kind, cb.face, cb.profile = b.kind, b.face, b.profile
+            for i in range(6):
+                cb.box[i] = int(b.box[i])
+            cb.value, cb.amp, cb.period = b.value, b.amp, b.period
+        c.objective = self.objective
+        for i in range(6):
+            c.obj_in[i] = int(self.obj_in[i])
+            c.obj_out[i] = int(self.obj_out[i])
+        c.obj_weight = self.obj_weight
+        return c
+
+
+class LBMError(RuntimeError):
+    def __init__(self, code: int, text: str):
+        super().__init__("%s (%d): %s" % (STATUS_TEXT.get(code, "error"), code, text))
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None) -> C.CDLL:
+    """Load liblbmgpu.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError("liblbmgpu.so not built at %s (run __graft_entry__.build())" % p)
+    lib = C.CDLL(p)
+    dp = C.POINTER(C.c_double)
+    H = C.c_void_p
+    sig = {
+        "lbm_config_default": (None, [C.POINTER(CConfig)]),
+        "lbm_create": (C.c_int, [C.POINTER(CConfig), C.POINTER(H)]),
+        "lbm_destroy": (C.c_int, [H]),
+        "lbm_last_error": (C.c_char_p, [H]),
+        "lbm_get_sizes": (C.c_int, [H, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+        "lbm_set_design": (C.c_int, [H, dp]),
+        "lbm_init_equilibrium": (C.c_int, [H, dp]),
+        "lbm_forward": (C.c_int, [H, C.c_int, dp, dp]),
+        "lbm_get_time": (C.c_int, [H, C.POINTER(C.c_int)]),
+        "lbm_get_populations": (C.c_int, [H, dp]),
+        "lbm_set_populations": (C.c_int, [H, dp, C.c_int]),
+        "lbm_get_macros": (C.c_int, [H, dp]),
+        "lbm_adjoint_reset": (C.c_int, [H]),
+        "lbm_adjoint_step": (C.c_int, [H]),
+        "lbm_get_adjoint": (C.c_int, [H, dp]),
+        "lbm_get_sensitivity": (C.c_int, [H, dp]),
+        "lbm_gradient": (C.c_int, [H, C.c_int, C.c_int, dp, dp, C.POINTER(CGradStats)]),
+        "lbm_time_steps": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+        "lbm_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
+        "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def wang_recompute_count(nsteps: int, nsnapshots: int) -> int:
+    lib = load_library()
+    out = C.c_int64()
+    rc = lib.lbm_wang_recompute_count(nsteps, nsnapshots, C.byref(out))
+    if rc:
+        raise LBMError(rc, lib.lbm_last_error(None).decode())
+    return out.value
+
+
+class Handle:
+    """Owns one lbm_handle (device-resident lattice)."""
+
+    def __init__(self, cfg: Config):
+        self.lib = load_library()
+        self.cfg = cfg
+        self._c = cfg.to_c()
+        h = C.c_void_p()
+        rc = self.lib.lbm_create(C.byref(self._c), C.byref(h))
+        if rc:
+            raise LBMError(rc, self.lib.lbm_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc:
+            raise LBMError(rc, self.lib.lbm_last_error(self.h).decode())
+
+    # -- forward ---------------------------------------------------------------
+    def set_design(self, gamma: np.ndarray):
+        g = np.ascontiguousarray(gamma, dtype=np.float64).ravel()
+        if g.size != self.cfg.ncells:
+            raise ValueError("gamma has %d values, expected %d" % (g.size, self.cfg.ncells))
+        self._check(self.lib.lbm_set_design(self.h, _ptr(g)))
+
+    def init_equilibrium(self, macros: Optional[np.ndarray] = None):
+        m = None if macros is None else np.ascontiguousarray(macros, dtype=np.float64).ravel()
+        self._check(self.lib.lbm_init_equilibrium(self.h, _ptr(m)))
+
+    def forward(self, nsteps: int, per_step: bool = False):
+        js = np.zeros(max(nsteps, 1)) if per_step else None
+        tot = np.zeros(1)
+        self._check(self.lib.lbm_forward(self.h, int(nsteps), _ptr(js), _ptr(tot)))
+        return (float(tot[0]), js[:nsteps]) if per_step else float(tot[0])
+
+    def time(self) -> int:
+        t = C.c_int()
+        self._check(self.lib.lbm_get_time(self.h, C.byref(t)))
+        return t.value
+
+    def populations(self) -> np.ndarray:
+        f = np.empty(self.cfg.ncells * self.cfg.npop)
+        self._check(self.lib.lbm_get_populations(self.h, _ptr(f)))
+        return f
+
+    def set_populations(self, f: np.ndarray, t: int):
+        a = np.ascontiguousarray(f, dtype=np.float64).ravel()
+        if a.size != self.cfg.ncells * self.cfg.npop:
+            raise ValueError("wrong population count")
+        self._check(self.lib.lbm_set_populations(self.h, _ptr(a), int(t)))
+
+    def macros(self) -> np.ndarray:
+        m = np.empty(self.cfg.ncells * self.cfg.nmac)
+        self._check(self.lib.lbm_get_macros(self.h, _ptr(m)))
+        return m
+
+    # -- adjoint ---------------------------------------------------------------
+    def adjoint_reset(self):
+        self._check(self.lib.lbm_adjoint_reset(self.h))
+
+    def adjoint_step(self):
+        self._check(self.lib.lbm_adjoint_step(self.h))
+
+    def adjoint(self) -> np.ndarray:
+        a = np.empty(self.cfg.ncells * self.cfg.npop)
+        self._check(self.lib.lbm_get_adjoint(self.h, _ptr(a)))
+        return a
+
+    def sensitivity(self) -> np.ndarray:
+        s = np.empty(self.cfg.ncells)
+        self._check(self.lib.lbm_get_sensitivity(self.h, _ptr(s)))
+        return s
+
+    def gradient(self, nsteps: int, nsnapshots: int):
+        J = np.zeros(1)
+        s = np.empty(self.cfg.ncells)
+        st = CGradStats()
+        self._check(self.lib.lbm_gradient(self.h, int(nsteps), int(nsnapshots), _ptr(J),
+                                          _ptr(s), C.byref(st)))
+        return float(J[0]), s, st
+
+    def time_steps(self, which: int, nsteps: int) -> float:
+        ms = C.c_float()
+        self._check(self.lib.lbm_time_steps(self.h, int(which), int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.lbm_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+
+# -- reference-style facades -----------------------------------------------------
+
+class IsothermalLBSolver:
+    """Mirror of IsothermalLBSolver2d/3d (latticeBoltzmann/isothermalLBSolver2d.hh:20-110)."""
+
+    def __init__(self, cfg: Config):
+        self.handle = Handle(cfg)
+
+    def setFieldFromDesignVec(self, gamma):
+        self.handle.set_design(gamma)
+
+    def initializeAtEquilibrium(self, macros=None):
+        self.handle.init_equilibrium(macros)
+
+    def collideAndStream(self, nsteps: int = 1) -> float:
+        return self.handle.forward(nsteps)
+
+    def getDistributions(self):
+        return self.handle.populations()
+
+    def setDistributions(self, f, t):
+        self.handle.set_populations(f, t)
+
+    def getCurrentTimestep(self) -> int:
+        return self.handle.time()
+
+
+class AdjointLBSolver:
+    """Mirror of AdjointLBSolver (adjointLatticeBoltzmann/adjointLBSolver.hh:11-46)."""
+
+    def __init__(self, solver: IsothermalLBSolver):
+        self.handle = solver.handle
+
+    def resetAdjoints(self):
+        self.handle.adjoint_reset()
+
+    def adjointStep(self):
+        self.handle.adjoint_step()
+
+    def getSensitivities(self):
+        return self.handle.sensitivity()
+
+
+class LBDynamicCheckpointing:
+    """Checkpointed forward+adjoint with Wang et al. dynamic checkpointing
+    (topOpt/LBCheckpointing.cc:322-351) and nsnapshots device slots."""
+
+    def __init__(self, nsnapshots: int, solver: IsothermalLBSolver):
+        self.k = int(nsnapshots)
+        self.solver = solver
+
+    def gradient(self, nsteps: int):
+        return self.solver.handle.gradient(nsteps, self.k)

@@ -1,0 +1,46 @@
+/*
+ * lbm_oracle.h -- CPU restatement of the reference LBM hot path (FP64).
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline arm as the checker.  Never linked by the product.
+ *
+ * All arrays are FP64 in DMDA order (cell c = (z*ny+y)*nx+x, AoS c*Q+q).
+ * Return 0 on success, negative on error.
+ */
+#ifndef LBM_ORACLE_H
+#define LBM_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/lbmgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int orc_sizes(const lbm_config* cfg, int64_t* ncell, int* npop, int* nmac);
+int orc_init(const lbm_config* cfg, const double* macros, double* f0);
+/* f holds f_{t0} on entry and f_{t0+nsteps} on exit. */
+int orc_forward_from(const lbm_config* cfg, const double* gamma, double* f, int t0, int nsteps,
+                     double* J_steps, double* J_sum);
+int orc_forward(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
+                double* f_out, double* J_steps, double* J_sum);
+/* One reverse step at f_t; lam (adjoint of the post-collision state of step t)
+ * is replaced by the one of step t-1; sens accumulates. */
+int orc_adjoint_step(const lbm_config* cfg, const double* gamma, const double* f_t, int t,
+                     double* lam, double* sens);
+int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
+                 double* J_sum, double* sens);
+int orc_macros(const lbm_config* cfg, const double* f, double* mac);
+int orc_collide_cell(const lbm_config* cfg, const double* fin, double gamma, double* fout,
+                     double* mac);
+int orc_reverse_cell(const lbm_config* cfg, const double* fin, double gamma,
+                     const double* lam_out, double* lam_in, double* dgamma);
+int orc_objective(const lbm_config* cfg, const double* f, const double* gamma, double* J);
+int orc_wang_count(int nsteps, int nsnap, int64_t* recomputed, int* ok);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,143 @@
+"""ctypes access to the CPU checkers: the C restatement (oracle/liblbmoracle.so)
+and, where it was built, the reference's own operators (oracle/_ref/libref.so).
+Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "lbm-topopt_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+
+from lbmgpu import CConfig, Config  # noqa: E402
+
+ORACLE_SO = os.path.join(ROOT, "oracle", "liblbmoracle.so")
+REF_SO = os.path.join(ROOT, "oracle", "_ref", "libref.so")
+
+_dp = C.POINTER(C.c_double)
+
+
+def _bind(lib, prefix):
+    cp = C.POINTER(CConfig)
+    sig = {
+        "forward": (C.c_int, [cp, _dp, _dp, C.c_int, _dp, _dp, _dp]),
+        "gradient": (C.c_int, [cp, _dp, _dp, C.c_int, _dp, _dp]),
+        "adjoint_step": (C.c_int, [cp, _dp, _dp, C.c_int, _dp, _dp]),
+        "collide_cell": (C.c_int, [cp, _dp, C.c_double, _dp, _dp]),
+        "reverse_cell": (C.c_int, [cp, _dp, C.c_double, _dp, _dp, _dp]),
+    }
+    for k, (r, a) in sig.items():
+        fn = getattr(lib, prefix + k)
+        fn.restype, fn.argtypes = r, a
+    if prefix == "orc_":
+        lib.orc_wang_count.restype = C.c_int
+        lib.orc_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+        lib.orc_forward_from.restype = C.c_int
+        lib.orc_forward_from.argtypes = [cp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
+        lib.orc_init.restype = C.c_int
+        lib.orc_init.argtypes = [cp, _dp, _dp]
+        lib.orc_macros.restype = C.c_int
+        lib.orc_macros.argtypes = [cp, _dp, _dp]
+        lib.orc_objective.restype = C.c_int
+        lib.orc_objective.argtypes = [cp, _dp, _dp, _dp]
+    else:
+        lib.ref_wang_count.restype = C.c_int
+        lib.ref_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_longlong),
+                                       C.POINTER(C.c_int)]
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+class Checker:
+    """Same calls for both libraries."""
+
+    def __init__(self, path: str, prefix: str):
+        self.lib = _bind(C.CDLL(path), prefix)
+        self.prefix = prefix
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def forward(self, cfg: Config, gamma, nsteps, macros=None):
+        c = cfg.to_c()
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        f = np.zeros(cfg.ncells * cfg.npop)
+        js = np.zeros(max(nsteps, 1))
+        tot = np.zeros(1)
+        m = None if macros is None else np.ascontiguousarray(macros, dtype=np.float64)
+        rc = self._fn("forward")(C.byref(c), _p(g), _p(m), int(nsteps), _p(f), _p(js), _p(tot))
+        if rc:
+            raise RuntimeError("%sforward failed: %d" % (self.prefix, rc))
+        return f, js[:nsteps], float(tot[0])
+
+    def gradient(self, cfg: Config, gamma, nsteps, macros=None):
+        c = cfg.to_c()
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        s = np.zeros(cfg.ncells)
+        tot = np.zeros(1)
+        m = None if macros is None else np.ascontiguousarray(macros, dtype=np.float64)
+        rc = self._fn("gradient")(C.byref(c), _p(g), _p(m), int(nsteps), _p(tot), _p(s))
+        if rc:
+            raise RuntimeError("%sgradient failed: %d" % (self.prefix, rc))
+        return float(tot[0]), s
+
+    def adjoint_step(self, cfg: Config, gamma, f_t, t, lam, sens):
+        c = cfg.to_c()
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        f = np.ascontiguousarray(f_t, dtype=np.float64)
+        lam = np.array(lam, dtype=np.float64)
+        sens = np.array(sens, dtype=np.float64)
+        rc = self._fn("adjoint_step")(C.byref(c), _p(g), _p(f), int(t), _p(lam), _p(sens))
+        if rc:
+            raise RuntimeError("adjoint_step failed: %d" % rc)
+        return lam, sens
+
+    def collide_cell(self, cfg: Config, fin, gamma):
+        c = cfg.to_c()
+        fin = np.ascontiguousarray(fin, dtype=np.float64)
+        fout = np.zeros(cfg.npop)
+        mac = np.zeros(4)
+        rc = self._fn("collide_cell")(C.byref(c), _p(fin), float(gamma), _p(fout), _p(mac))
+        if rc:
+            raise RuntimeError("collide_cell failed: %d" % rc)
+        return fout, mac[:cfg.nmac]
+
+    def reverse_cell(self, cfg: Config, fin, gamma, lam_out):
+        c = cfg.to_c()
+        fin = np.ascontiguousarray(fin, dtype=np.float64)
+        lo = np.ascontiguousarray(lam_out, dtype=np.float64)
+        li = np.zeros(cfg.npop)
+        dg = np.zeros(1)
+        rc = self._fn("reverse_cell")(C.byref(c), _p(fin), float(gamma), _p(lo), _p(li), _p(dg))
+        if rc:
+            raise RuntimeError("reverse_cell failed: %d" % rc)
+        return li, float(dg[0])
+
+    def wang_count(self, nsteps, nsnap):
+        if self.prefix == "orc_":
+            r, ok = C.c_int64(), C.c_int()
+        else:
+            r, ok = C.c_longlong(), C.c_int()
+        rc = self._fn("wang_count")(int(nsteps), int(nsnap), C.byref(r), C.byref(ok))
+        if rc:
+            raise RuntimeError("wang_count failed: %d" % rc)
+        return int(r.value), bool(ok.value)
+
+
+def oracle() -> Checker:
+    return Checker(ORACLE_SO, "orc_")
+
+
+def reference():
+    """The reference build, or None where it was not built (no reference tree)."""
+    if not os.path.exists(REF_SO):
+        return None
+    return Checker(REF_SO, "ref_")
