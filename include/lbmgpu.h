@@ -64,7 +64,6 @@ extern "C" {
 #define LBM_BC_VELOCITY    1  /* Zou-He (2D, ZouHe2d.hh:23-56) / Hecht (3D, Hecht3d.hh:62-94) */
 #define LBM_BC_PRESSURE    2  /* Zou-He (ZouHe2d.hh:245-281) / Hecht (Hecht3d.hh:175-209) */
 #define LBM_BC_TEMPERATURE 3  /* thermal Zou-He Dirichlet (thermalZouHe2d.hh:63-97) */
-#define LBM_BC_THERMAL_NEUMANN 4 /* zero-gradient outflow of the temperature lattice */
 
 /* Faces.  West = x min, East = x max, South = y min, North = y max,
  * Bottom = z min, Top = z max. */
@@ -182,9 +181,12 @@ int lbm_get_macros(const lbm_handle* h, double* mac);
  * Replaces AdjointLBSolver::resetAdjoints (adjointLBSolver.cc:138-145). */
 int lbm_adjoint_reset(lbm_handle* h);
 
-/* One reverse time step for the forward state currently held (f_t, t >= 1):
+/* One reverse time step for the forward state currently held (f_t):
  * adjoint collision at f_t with sensitivity accumulation, objective source
- * weight*dF/df_t, adjoint boundary conditions at t, adjoint stream.
+ * weight*dF/df_t, adjoint boundary conditions at t, adjoint stream.  At t = 0
+ * only the adjoint collision runs (no objective, no boundary): the design
+ * dependence of the first collision, which the reference's reverse loop
+ * (applications/RobustPump2d/robustPump2d.cc:268-276) leaves out.
  * Replaces AdjointLBSolver::adjointCollide + computeCollideSource +
  * computeSensitivitySource + adjointStream (adjointLBSolver.cc:28-122). */
 int lbm_adjoint_step(lbm_handle* h);
@@ -200,7 +202,8 @@ int lbm_get_sensitivity(const lbm_handle* h, double* sens);
 
 /* Full gradient: f_0 from uniform rest (or the macros of the last
  * lbm_init_equilibrium), nsteps forward steps with Wang et al. dynamic
- * checkpointing in nsnapshots device slots, then the reverse sweep.
+ * checkpointing in nsnapshots device slots, then the reverse sweep, closed by
+ * the reverse of the collision of f_0 (see lbm_adjoint_step).
  * Replaces the checkpointed driver of robustPump2d.cc:234-276 with
  * LBDynamicCheckpointing (topOpt/LBCheckpointing.cc:322-351,
  * topOpt/dynamicCheckpointing.cc:9-54, topOpt/WangCheckpointing.cc:36-126).

@@ -1,0 +1,21 @@
+// kernels_d2q9.cu -- instantiation of the step kernels for one lattice.
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+
+#define LAT LAT_D2Q9
+LaunchFn launcher_d2q9(int collision, int storage) {
+  if (collision == LBM_BGK) {
+    if (storage == LBM_STORE_FP64) return &OpsImpl<LAT, LBM_BGK, double>::launch;
+    if (storage == LBM_STORE_FP32) return &OpsImpl<LAT, LBM_BGK, float>::launch;
+    if (storage == LBM_STORE_FP16) return &OpsImpl<LAT, LBM_BGK, __half>::launch;
+  } else if (collision == LBM_MRT) {
+    if (storage == LBM_STORE_FP64) return &OpsImpl<LAT, LBM_MRT, double>::launch;
+    if (storage == LBM_STORE_FP32) return &OpsImpl<LAT, LBM_MRT, float>::launch;
+    if (storage == LBM_STORE_FP16) return &OpsImpl<LAT, LBM_MRT, __half>::launch;
+  }
+  return nullptr;
+}
+#undef LAT
+
+}  // namespace lbm

@@ -1,0 +1,756 @@
+// lbm_capi.cu -- the C ABI of include/lbmgpu.h: handle life cycle, argument
+// checking, device memory, the time-stepping drivers and the checkpointed
+// gradient.  All numerical work is done by the kernels of kernels_*.cu; there
+// is no host fallback.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbmgpu.h"
+#include "lbm_device.cuh"
+#include "lbm_ops.h"
+#include "wang.hpp"
+
+using namespace lbm;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+const int kBlockThreads = 256;
+
+struct Geometry {
+  dim3 grid, block;
+  unsigned nblocks;
+};
+
+}  // namespace
+
+struct lbm_handle {
+  lbm_config cfg;
+  int Q = 0, QF = 0, nmac = 0, dim = 2;
+  int64_t ncell = 0;
+  long long P = 0;       // plane stride (elements)
+  size_t pop_bytes = 0;  // bytes per population value
+  size_t adj_bytes = 0;  // bytes per adjoint value
+  size_t gam_bytes = 0;  // bytes per design value
+  LaunchFn launch = nullptr;
+  cudaStream_t stream = nullptr;
+  Geometry geo;
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  void* gamma = nullptr;
+  void* lam[2] = {nullptr, nullptr};
+  int lcur = 0;
+  double* sens = nullptr;
+  double* partial = nullptr;
+  unsigned* counter = nullptr;
+  double* jdev = nullptr;
+  size_t jcap = 0;
+  double* stage = nullptr;     // FP64 AoS staging (ncell*Q)
+  double* init_mac = nullptr;  // initial macros kept for lbm_gradient (device, may be null)
+  std::vector<void*> slots;
+  int t = 0;
+  bool have_design = false, have_state = false, have_adjoint = false;
+  int64_t launches = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string err;
+};
+
+namespace {
+
+int fail(lbm_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h)
+    h->err = buf;
+  else
+    g_create_error = buf;
+  return code;
+}
+
+#define CUDA_OR_FAIL(h, call)                                                              \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail((h), LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t state_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->pop_bytes; }
+size_t adjoint_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->adj_bytes; }
+
+int check_box(const lbm_config& c, const int* b, int dim, const char* what) {
+  int nz = dim == 3 ? c.nz : 1;
+  if (b[0] < 0 || b[1] >= c.nx || b[0] > b[1] || b[2] < 0 || b[3] >= c.ny || b[2] > b[3] ||
+      b[4] < 0 || b[5] >= nz || b[4] > b[5])
+    return fail(nullptr, LBM_ERR_ARG, "%s box [%d,%d]x[%d,%d]x[%d,%d] outside the %dx%dx%d lattice",
+                what, b[0], b[1], b[2], b[3], b[4], b[5], c.nx, c.ny, nz);
+  return 0;
+}
+
+int validate(const lbm_config& c) {
+  if (c.lattice != LBM_D2Q9 && c.lattice != LBM_D3Q19 && c.lattice != LBM_D2Q9_D2Q5)
+    return fail(nullptr, LBM_ERR_ARG, "unknown lattice %d", c.lattice);
+  if (c.collision != LBM_BGK && c.collision != LBM_MRT)
+    return fail(nullptr, LBM_ERR_ARG, "unknown collision %d", c.collision);
+  if (c.storage != LBM_STORE_FP64 && c.storage != LBM_STORE_FP32 && c.storage != LBM_STORE_FP16)
+    return fail(nullptr, LBM_ERR_ARG, "unknown storage %d", c.storage);
+  if (c.lattice == LBM_D2Q9_D2Q5 && (c.collision != LBM_BGK || c.storage == LBM_STORE_FP16))
+    return fail(nullptr, LBM_ERR_SUP,
+                "the thermal lattice supports BGK flow with FP64 or FP32 storage only");
+  int dim = c.lattice == LBM_D3Q19 ? 3 : 2;
+  if (c.nx < 3 || c.ny < 3 || (dim == 3 && c.nz < 3))
+    return fail(nullptr, LBM_ERR_ARG, "lattice %dx%dx%d too small (>= 3 cells per axis)", c.nx,
+                c.ny, c.nz);
+  if ((double)c.nx * c.ny * (dim == 3 ? c.nz : 1) > 2.0e9)
+    return fail(nullptr, LBM_ERR_ARG, "lattice too large");
+  if (!(c.omega > 0. && c.omega < 2.))
+    return fail(nullptr, LBM_ERR_ARG, "omega %g outside (0,2)", c.omega);
+  if (!(c.interp_q > 0.) || !std::isfinite(c.interp_scale))
+    return fail(nullptr, LBM_ERR_ARG, "interpolation q must be > 0");
+  if (c.lattice == LBM_D2Q9_D2Q5 && (!(c.diffusivity > 0.) || !(c.ramp_ck > 0.) || !(c.ramp_q >= 0.)))
+    return fail(nullptr, LBM_ERR_ARG, "thermal lattice needs diffusivity > 0, ramp_ck > 0, ramp_q >= 0");
+  if (c.nbc < 0 || c.nbc > LBM_MAX_BC)
+    return fail(nullptr, LBM_ERR_ARG, "nbc %d outside [0,%d]", c.nbc, LBM_MAX_BC);
+  for (int k = 0; k < c.nbc; ++k) {
+    const lbm_bc& b = c.bc[k];
+    int rc = check_box(c, b.box, dim, "boundary");
+    if (rc) return rc;
+    bool ok = false;
+    if (b.kind == LBM_BC_VELOCITY || b.kind == LBM_BC_PRESSURE) {
+      if (b.face == LBM_FACE_WEST) ok = (b.box[0] == 0 && b.box[1] == 0);
+      if (b.face == LBM_FACE_EAST) ok = (b.box[0] == c.nx - 1 && b.box[1] == c.nx - 1);
+      if (dim == 3 && !((b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) ||
+                        (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_EAST)))
+        return fail(nullptr, LBM_ERR_SUP,
+                    "D3Q19 supports the Hecht velocity west and pressure east faces only");
+    } else if (b.kind == LBM_BC_TEMPERATURE) {
+      if (c.lattice != LBM_D2Q9_D2Q5)
+        return fail(nullptr, LBM_ERR_SUP, "temperature boundary needs the thermal lattice");
+      ok = (b.face == LBM_FACE_WEST && b.box[0] == 0 && b.box[1] == 0);
+    } else {
+      return fail(nullptr, LBM_ERR_SUP, "boundary kind %d not supported", b.kind);
+    }
+    if (!ok) return fail(nullptr, LBM_ERR_ARG, "boundary %d: box does not lie on its face", k);
+    if (b.amp != 0. && !(b.period > 0.))
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: oscillation needs period > 0", k);
+    if (!std::isfinite(b.value)) return fail(nullptr, LBM_ERR_ARG, "boundary %d: bad value", k);
+  }
+  if (c.objective == LBM_OBJ_PRESSURE_DROP) {
+    int rc = check_box(c, c.obj_in, dim, "objective inflow");
+    if (rc) return rc;
+    rc = check_box(c, c.obj_out, dim, "objective outflow");
+    if (rc) return rc;
+  } else if (c.objective == LBM_OBJ_HEAT_FLUX) {
+    if (c.lattice != LBM_D2Q9_D2Q5)
+      return fail(nullptr, LBM_ERR_SUP, "heat flux objective needs the thermal lattice");
+    int rc = check_box(c, c.obj_out, dim, "objective outflow");
+    if (rc) return rc;
+  } else if (c.objective != LBM_OBJ_NONE && c.objective != LBM_OBJ_DISSIPATION) {
+    return fail(nullptr, LBM_ERR_ARG, "unknown objective %d", c.objective);
+  }
+  return 0;
+}
+
+void destroy_buffers(lbm_handle* h) {
+  for (void*& p : h->f) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  for (void*& p : h->lam) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  for (void* s : h->slots)
+    if (s) cudaFree(s);
+  h->slots.clear();
+  void* ps[] = {h->gamma, h->sens, h->partial, h->counter, h->jdev, h->stage, h->init_mac};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  h->gamma = h->sens = h->partial = nullptr;
+  h->counter = nullptr;
+  h->jdev = h->stage = h->init_mac = nullptr;
+  for (cudaEvent_t& e : h->ev)
+    if (e) {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
+  if (h->stream) cudaStreamDestroy(h->stream);
+  h->stream = nullptr;
+}
+
+KParams base_params(const lbm_handle* h, int t) {
+  const lbm_config& c = h->cfg;
+  KParams p;
+  memset(&p, 0, sizeof(p));
+  p.nx = c.nx;
+  p.ny = c.ny;
+  p.nz = h->dim == 3 ? c.nz : 1;
+  p.P = h->P;
+  p.omega = c.omega;
+  for (int i = 0; i < 8; ++i) p.mrt[i] = c.mrt[i];
+  p.pbb_scale = c.interp_scale;
+  p.pbb_q = c.interp_q;
+  p.diff = c.diffusivity;
+  p.ramp_q = c.ramp_q;
+  p.ramp_ck = c.ramp_ck;
+  p.heat_rate = c.heat_rate;
+  p.heat_T = c.heat_T;
+  p.nbc = c.nbc;
+  p.apply_bc = t >= 1;
+  for (int k = 0; k < c.nbc; ++k) {
+    const lbm_bc& b = c.bc[k];
+    DevBC& d = p.bc[k];
+    d.kind = b.kind;
+    d.face = b.face;
+    d.profile = b.profile;
+    for (int i = 0; i < 6; ++i) d.box[i] = b.box[i];
+    // value(t) = value * (1 + amp sin(2 pi t / period)), evaluated here once per launch
+    double tf = (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
+    d.value = b.value * tf;
+  }
+  p.objective = c.objective;
+  p.obj_weight = c.obj_weight;
+  for (int i = 0; i < 6; ++i) {
+    p.obj_in[i] = c.obj_in[i];
+    p.obj_out[i] = c.obj_out[i];
+  }
+  if (c.objective == LBM_OBJ_PRESSURE_DROP) {
+    const int* a = c.obj_in;
+    const int* b = c.obj_out;
+    p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
+    p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
+  }
+  p.partial = h->partial;
+  p.counter = h->counter;
+  p.gamma = h->gamma;
+  p.sens = h->sens;
+  return p;
+}
+
+int launch(lbm_handle* h, int kind, const KParams& p, double* aux) {
+  h->launch(kind, h->geo.grid, h->geo.block, h->stream, p, aux);
+  h->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "kernel launch %d: %s", kind, cudaGetErrorString(e));
+  return 0;
+}
+
+int ensure_jcap(lbm_handle* h, size_t n) {
+  if (n <= h->jcap) return 0;
+  if (h->jdev) cudaFree(h->jdev);
+  h->jdev = nullptr;
+  size_t cap = n < 1024 ? 1024 : n;
+  CUDA_OR_FAIL(h, cudaMalloc(&h->jdev, cap * sizeof(double)));
+  h->jcap = cap;
+  return 0;
+}
+
+int ensure_stage(lbm_handle* h) {
+  if (h->stage) return 0;
+  CUDA_OR_FAIL(h, cudaMalloc(&h->stage, (size_t)h->ncell * h->Q * sizeof(double)));
+  return 0;
+}
+
+// One forward step f~_t -> f~_{t+1}; result (may be null) receives F(f_t).
+int forward_step(lbm_handle* h, double* result) {
+  KParams p = base_params(h, h->t);
+  p.fin = h->f[h->cur];
+  p.fout = h->f[1 - h->cur];
+  p.eval_obj = (result != nullptr && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+  p.result = result;
+  int rc = launch(h, K_FORWARD, p, nullptr);
+  if (rc) return rc;
+  h->cur ^= 1;
+  h->t += 1;
+  return 0;
+}
+
+int objective_only(lbm_handle* h, double* result) {
+  KParams p = base_params(h, h->t);
+  p.fin = h->f[h->cur];
+  p.eval_obj = 1;
+  p.result = result;
+  return launch(h, K_OBJECTIVE, p, nullptr);
+}
+
+// One reverse step at the current forward state f_t.
+int adjoint_step(lbm_handle* h) {
+  KParams p = base_params(h, h->t);
+  p.fin = h->f[h->cur];
+  p.lam_in = h->lam[h->lcur];
+  p.lam_out = h->lam[1 - h->lcur];
+  p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+  int rc = launch(h, K_ADJOINT, p, nullptr);
+  if (rc) return rc;
+  h->lcur ^= 1;
+  return 0;
+}
+
+int sync(lbm_handle* h) {
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "device error: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int zero_adjoint(lbm_handle* h) {
+  for (void* p : h->lam) CUDA_OR_FAIL(h, cudaMemsetAsync(p, 0, adjoint_bytes(h), h->stream));
+  CUDA_OR_FAIL(h, cudaMemsetAsync(h->sens, 0, (size_t)h->ncell * sizeof(double), h->stream));
+  h->lcur = 0;
+  return 0;
+}
+
+int init_state(lbm_handle* h) {
+  KParams p = base_params(h, 0);
+  p.fout = h->f[h->cur];
+  int rc = launch(h, K_INIT, p, h->init_mac);
+  if (rc) return rc;
+  h->t = 0;
+  h->have_state = true;
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+
+extern "C" {
+
+void lbm_config_default(lbm_config* c) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->lattice = LBM_D2Q9;
+  c->collision = LBM_BGK;
+  c->storage = LBM_STORE_FP64;
+  c->nx = c->ny = c->nz = 1;
+  c->omega = 1.;
+  const double d3[8] = {1.19, 1.4, 1.2, 1.4, 1.4, 3., -5.5, -0.5};
+  for (int i = 0; i < 8; ++i) c->mrt[i] = d3[i];
+  c->interp_scale = 1.;
+  c->interp_q = 1.;
+  c->ramp_q = 1.;
+  c->ramp_ck = 1.;
+  c->heat_T = 1.;
+  c->obj_weight = 1.;
+}
+
+const char* lbm_last_error(const lbm_handle* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int lbm_create(const lbm_config* cfg, lbm_handle** out) {
+  if (!cfg || !out) return fail(nullptr, LBM_ERR_ARG, "null argument");
+  *out = nullptr;
+  int rc = validate(*cfg);
+  if (rc) return rc;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, LBM_ERR_CUDA, "no CUDA device available (%s)",
+                e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+  lbm_handle* h = new (std::nothrow) lbm_handle();
+  if (!h) return fail(nullptr, LBM_ERR_MEM, "host allocation failed");
+  h->cfg = *cfg;
+  const lbm_config& c = h->cfg;
+  h->dim = c.lattice == LBM_D3Q19 ? 3 : 2;
+  if (h->dim == 2) h->cfg.nz = 1;
+  h->Q = c.lattice == LBM_D2Q9 ? 9 : c.lattice == LBM_D3Q19 ? 19 : 14;
+  h->QF = c.lattice == LBM_D3Q19 ? 19 : 9;
+  h->nmac = c.lattice == LBM_D2Q9 ? 3 : 4;
+  h->ncell = (int64_t)c.nx * c.ny * h->cfg.nz;
+  h->P = (h->ncell + 127) / 128 * 128;
+  h->pop_bytes = c.storage == LBM_STORE_FP64 ? 8 : c.storage == LBM_STORE_FP32 ? 4 : 2;
+  h->adj_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
+  h->gam_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
+  h->launch = c.lattice == LBM_D2Q9    ? launcher_d2q9(c.collision, c.storage)
+              : c.lattice == LBM_D3Q19 ? launcher_d3q19(c.collision, c.storage)
+                                       : launcher_thermal(c.collision, c.storage);
+  if (!h->launch) {
+    delete h;
+    return fail(nullptr, LBM_ERR_SUP, "no kernel for lattice %d collision %d storage %d",
+                c.lattice, c.collision, c.storage);
+  }
+  // thread blocks: 256 threads, x-major rows
+  int bx = c.nx >= 256 ? 256 : ((c.nx + 31) / 32) * 32;
+  if (bx > 256) bx = 256;
+  int by = kBlockThreads / bx;
+  if (by < 1) by = 1;
+  h->geo.block = dim3(bx, by, 1);
+  h->geo.grid = dim3((c.nx + bx - 1) / bx, (c.ny + by - 1) / by, h->cfg.nz);
+  h->geo.nblocks = h->geo.grid.x * h->geo.grid.y * h->geo.grid.z;
+
+#define ALLOC(ptr, bytes)                                                                  \
+  do {                                                                                     \
+    cudaError_t ee = cudaMalloc((void**)&(ptr), (bytes));                                  \
+    if (ee != cudaSuccess) {                                                               \
+      destroy_buffers(h);                                                                  \
+      delete h;                                                                            \
+      return fail(nullptr, ee == cudaErrorMemoryAllocation ? LBM_ERR_MEM : LBM_ERR_CUDA,   \
+                  "cudaMalloc(%zu bytes): %s", (size_t)(bytes), cudaGetErrorString(ee));    \
+    }                                                                                      \
+  } while (0)
+
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return fail(nullptr, LBM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (int i = 0; i < 4; ++i) cudaEventCreate(&h->ev[i]);
+  ALLOC(h->f[0], state_bytes(h));
+  ALLOC(h->f[1], state_bytes(h));
+  ALLOC(h->lam[0], adjoint_bytes(h));
+  ALLOC(h->lam[1], adjoint_bytes(h));
+  ALLOC(h->gamma, (size_t)h->P * h->gam_bytes);
+  ALLOC(h->sens, (size_t)h->P * sizeof(double));
+  ALLOC(h->partial, (size_t)h->geo.nblocks * sizeof(double));
+  ALLOC(h->counter, sizeof(unsigned));
+#undef ALLOC
+  cudaMemsetAsync(h->counter, 0, sizeof(unsigned), h->stream);
+  cudaMemsetAsync(h->f[0], 0, state_bytes(h), h->stream);
+  cudaMemsetAsync(h->f[1], 0, state_bytes(h), h->stream);
+  if (zero_adjoint(h) || sync(h)) {
+    std::string msg = h->err;
+    destroy_buffers(h);
+    delete h;
+    return fail(nullptr, LBM_ERR_CUDA, "initialisation failed: %s", msg.c_str());
+  }
+  *out = h;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_handle* h) {
+  if (!h) return LBM_OK;
+  cudaStreamSynchronize(h->stream);
+  destroy_buffers(h);
+  delete h;
+  return LBM_OK;
+}
+
+int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (ncells) *ncells = h->ncell;
+  if (npop) *npop = h->Q;
+  return LBM_OK;
+}
+
+int lbm_set_design(lbm_handle* h, const double* gamma) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!gamma) return fail(h, LBM_ERR_ARG, "null design pointer");
+  for (int64_t i = 0; i < h->ncell; ++i) {
+    double g = gamma[i];
+    if (!std::isfinite(g)) return fail(h, LBM_ERR_NONFINITE, "design value %lld is not finite", (long long)i);
+    if (g < 0. || g > 1.) return fail(h, LBM_ERR_ARG, "design value %lld = %g outside [0,1]", (long long)i, g);
+  }
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(h->stage, gamma, (size_t)h->ncell * sizeof(double),
+                                  cudaMemcpyHostToDevice, h->stream));
+  KParams p = base_params(h, 0);
+  rc = launch(h, K_GAMMA, p, h->stage);
+  if (rc) return rc;
+  rc = sync(h);
+  if (rc) return rc;
+  h->have_design = true;
+  return LBM_OK;
+}
+
+int lbm_init_equilibrium(lbm_handle* h, const double* macros) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (macros) {
+    size_t n = (size_t)h->ncell * h->nmac;
+    for (size_t i = 0; i < n; ++i)
+      if (!std::isfinite(macros[i])) return fail(h, LBM_ERR_NONFINITE, "initial macro %zu not finite", i);
+    if (!h->init_mac) CUDA_OR_FAIL(h, cudaMalloc(&h->init_mac, n * sizeof(double)));
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(h->init_mac, macros, n * sizeof(double), cudaMemcpyHostToDevice,
+                                    h->stream));
+  } else if (h->init_mac) {
+    cudaFree(h->init_mac);
+    h->init_mac = nullptr;
+  }
+  int rc = init_state(h);
+  if (rc) return rc;
+  return sync(h);
+}
+
+int lbm_forward(lbm_handle* h, int nsteps, double* J_steps, double* J_sum) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (nsteps < 0) return fail(h, LBM_ERR_ARG, "nsteps %d < 0", nsteps);
+  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+  if (!h->have_state) return fail(h, LBM_ERR_STATE, "no state (lbm_init_equilibrium)");
+  if (J_sum) *J_sum = 0.;
+  if (nsteps == 0) return LBM_OK;
+  bool obj = h->cfg.objective != LBM_OBJ_NONE;
+  int rc = ensure_jcap(h, (size_t)nsteps);
+  if (rc) return rc;
+  for (int k = 0; k < nsteps; ++k) {
+    rc = forward_step(h, (obj && k > 0) ? h->jdev + (k - 1) : nullptr);
+    if (rc) return rc;
+  }
+  if (obj) {
+    rc = objective_only(h, h->jdev + (nsteps - 1));
+    if (rc) return rc;
+  }
+  rc = sync(h);
+  if (rc) return rc;
+  if (obj) {
+    std::vector<double> js((size_t)nsteps);
+    CUDA_OR_FAIL(h, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double acc = 0.;
+    for (int k = 0; k < nsteps; ++k) acc += js[k];
+    if (!std::isfinite(acc)) return fail(h, LBM_ERR_NONFINITE, "objective is not finite");
+    if (J_steps) memcpy(J_steps, js.data(), js.size() * sizeof(double));
+    if (J_sum) *J_sum = acc;
+  } else if (J_steps) {
+    memset(J_steps, 0, sizeof(double) * nsteps);
+  }
+  return LBM_OK;
+}
+
+int lbm_get_time(const lbm_handle* h, int* t) {
+  if (!h || !t) return fail(nullptr, LBM_ERR_ARG, "null argument");
+  *t = h->t;
+  return LBM_OK;
+}
+
+int lbm_get_populations(const lbm_handle* hc, double* f) {
+  lbm_handle* h = const_cast<lbm_handle*>(hc);
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!f) return fail(h, LBM_ERR_ARG, "null output");
+  if (!h->have_state) return fail(h, LBM_ERR_STATE, "no state");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  KParams p = base_params(h, h->t);
+  p.fin = h->f[h->cur];
+  rc = launch(h, K_EXPORT, p, h->stage);
+  if (rc) return rc;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(f, h->stage, (size_t)h->ncell * h->Q * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int lbm_set_populations(lbm_handle* h, const double* f, int t) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!f) return fail(h, LBM_ERR_ARG, "null input");
+  if (t < 0) return fail(h, LBM_ERR_ARG, "time step %d < 0", t);
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(h->stage, f, (size_t)h->ncell * h->Q * sizeof(double),
+                                  cudaMemcpyHostToDevice, h->stream));
+  KParams p = base_params(h, t);
+  p.fout = h->f[h->cur];
+  rc = launch(h, K_IMPORT, p, h->stage);
+  if (rc) return rc;
+  h->t = t;
+  h->have_state = true;
+  return sync(h);
+}
+
+int lbm_get_macros(const lbm_handle* hc, double* mac) {
+  lbm_handle* h = const_cast<lbm_handle*>(hc);
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!mac) return fail(h, LBM_ERR_ARG, "null output");
+  if (!h->have_state) return fail(h, LBM_ERR_STATE, "no state");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  KParams p = base_params(h, h->t);
+  p.fin = h->f[h->cur];
+  rc = launch(h, K_MACROS, p, h->stage);
+  if (rc) return rc;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(mac, h->stage, (size_t)h->ncell * h->nmac * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int lbm_adjoint_reset(lbm_handle* h) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  int rc = zero_adjoint(h);
+  if (rc) return rc;
+  h->have_adjoint = true;
+  return sync(h);
+}
+
+int lbm_adjoint_step(lbm_handle* h) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!h->have_design || !h->have_state) return fail(h, LBM_ERR_STATE, "no design or state");
+  if (!h->have_adjoint) return fail(h, LBM_ERR_STATE, "adjoint not reset (lbm_adjoint_reset)");
+  int rc = adjoint_step(h);
+  if (rc) return rc;
+  return sync(h);
+}
+
+int lbm_get_adjoint(const lbm_handle* hc, double* lam) {
+  lbm_handle* h = const_cast<lbm_handle*>(hc);
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!lam) return fail(h, LBM_ERR_ARG, "null output");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  KParams p = base_params(h, h->t);
+  p.lam_in = h->lam[h->lcur];
+  rc = launch(h, K_EXPORT_ADJ, p, h->stage);
+  if (rc) return rc;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(lam, h->stage, (size_t)h->ncell * h->Q * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int lbm_get_sensitivity(const lbm_handle* hc, double* sens) {
+  lbm_handle* h = const_cast<lbm_handle*>(hc);
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!sens) return fail(h, LBM_ERR_ARG, "null output");
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(sens, h->sens, (size_t)h->ncell * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgamma,
+                 lbm_gradient_stats* stats) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (nsteps < 1) return fail(h, LBM_ERR_ARG, "nsteps %d < 1", nsteps);
+  if (nsnap < 2) return fail(h, LBM_ERR_ARG, "nsnapshots %d < 2", nsnap);
+  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+  int rc;
+  // snapshot slots in device memory
+  if ((int)h->slots.size() != nsnap) {
+    for (void* s : h->slots)
+      if (s) cudaFree(s);
+    h->slots.assign(nsnap, nullptr);
+    for (int i = 0; i < nsnap; ++i) {
+      cudaError_t e = cudaMalloc(&h->slots[i], state_bytes(h));
+      if (e != cudaSuccess) {
+        for (void* s : h->slots)
+          if (s) cudaFree(s);
+        h->slots.clear();
+        return fail(h, LBM_ERR_MEM, "%d snapshot slots of %zu bytes: %s", nsnap, state_bytes(h),
+                    cudaGetErrorString(e));
+      }
+    }
+  }
+  if ((rc = ensure_jcap(h, (size_t)nsteps))) return rc;
+  const bool obj = h->cfg.objective != LBM_OBJ_NONE;
+  const size_t sb = state_bytes(h);
+  WangSchedule ws(nsnap);
+  auto save = [&](int slot) -> int {
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(h->slots[slot], h->f[h->cur], sb, cudaMemcpyDeviceToDevice, h->stream));
+    return 0;
+  };
+  WangSchedule::Actions act;
+  act.advance = [&]() { return forward_step(h, nullptr); };
+  act.restore = [&](int step, int slot) -> int {
+    CUDA_OR_FAIL(h, cudaMemcpyAsync(h->f[h->cur], h->slots[slot], sb, cudaMemcpyDeviceToDevice, h->stream));
+    h->t = step;
+    return 0;
+  };
+  act.save = save;
+
+  cudaEventRecord(h->ev[0], h->stream);
+  if ((rc = init_state(h))) return rc;
+  if ((rc = save(ws.make_checkpoint(0)))) return rc;
+  for (int s = 0; s < nsteps; ++s) {
+    if ((rc = forward_step(h, (obj && s >= 1) ? h->jdev + (s - 1) : nullptr))) return rc;
+    if ((rc = save(ws.make_checkpoint(s + 1)))) return rc;
+  }
+  if (obj && (rc = objective_only(h, h->jdev + (nsteps - 1)))) return rc;
+  cudaEventRecord(h->ev[1], h->stream);
+  if ((rc = zero_adjoint(h))) return rc;
+  h->have_adjoint = true;
+  for (int s = nsteps; s >= 1; --s) {
+    try {
+      rc = ws.get_forward_solution(s, act);
+    } catch (const std::exception& ex) {
+      return fail(h, LBM_ERR_STATE, "checkpoint schedule: %s", ex.what());
+    }
+    if (rc) return rc;
+    if ((rc = adjoint_step(h))) return rc;
+  }
+  // The collision of f_0 depends on the design too; the reference's reverse loop stops
+  // at step 1 (robustPump2d.cc:268-276).  Reverse it as well: no objective and no
+  // boundary at t = 0.  The term is exactly zero for isothermal flows started at rest.
+  if ((rc = init_state(h))) return rc;
+  if ((rc = adjoint_step(h))) return rc;
+  cudaEventRecord(h->ev[2], h->stream);
+  if ((rc = sync(h))) return rc;
+  double acc = 0.;
+  if (obj) {
+    std::vector<double> js((size_t)nsteps);
+    CUDA_OR_FAIL(h, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (double v : js) acc += v;
+    if (!std::isfinite(acc)) return fail(h, LBM_ERR_NONFINITE, "objective is not finite");
+  }
+  if (J) *J = acc;
+  if (dJdgamma) {
+    CUDA_OR_FAIL(h, cudaMemcpy(dJdgamma, h->sens, (size_t)h->ncell * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (stats) {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+    stats->forward_steps = nsteps;
+    stats->recomputed_steps = ws.recomputed();
+    stats->adjoint_steps = nsteps;
+    stats->forward_ms = a;
+    stats->reverse_ms = b;
+  }
+  return LBM_OK;
+}
+
+int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!ms || nsteps < 1 || (which != 0 && which != 1)) return fail(h, LBM_ERR_ARG, "bad arguments");
+  if (!h->have_design || !h->have_state) return fail(h, LBM_ERR_STATE, "no design or state");
+  int rc;
+  if (which == 1 && !h->have_adjoint) {
+    if ((rc = zero_adjoint(h))) return rc;
+    h->have_adjoint = true;
+  }
+  int t_keep = h->t;
+  if (which == 1 && h->t < 1) h->t = 1;
+  cudaEventRecord(h->ev[0], h->stream);
+  for (int k = 0; k < nsteps; ++k) {
+    rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
+    if (rc) return rc;
+  }
+  cudaEventRecord(h->ev[1], h->stream);
+  if ((rc = sync(h))) return rc;
+  if (which == 1) h->t = t_keep;
+  cudaEventElapsedTime(ms, h->ev[0], h->ev[1]);
+  return LBM_OK;
+}
+
+int lbm_get_launch_count(const lbm_handle* h, int64_t* n) {
+  if (!h || !n) return fail(nullptr, LBM_ERR_ARG, "null argument");
+  *n = h->launches;
+  return LBM_OK;
+}
+
+int lbm_wang_recompute_count(int nsteps, int nsnap, int64_t* recomputed) {
+  if (!recomputed || nsteps < 1 || nsnap < 2)
+    return fail(nullptr, LBM_ERR_ARG, "need nsteps >= 1, nsnapshots >= 2");
+  WangSchedule ws(nsnap);
+  std::vector<int> slot_step(nsnap, -1);
+  int state = 0;
+  for (int s = 0; s <= nsteps; ++s) slot_step[ws.make_checkpoint(s)] = s;
+  WangSchedule::Actions act;
+  act.advance = [&]() { ++state; return 0; };
+  act.restore = [&](int step, int slot) {
+    if (slot_step[slot] != step) return -1;
+    state = step;
+    return 0;
+  };
+  act.save = [&](int slot) { slot_step[slot] = state; return 0; };
+  for (int s = nsteps; s >= 1; --s) {
+    int rc = ws.get_forward_solution(s, act);
+    if (rc || state != s) return fail(nullptr, LBM_ERR_STATE, "schedule did not reverse at step %d", s);
+  }
+  *recomputed = ws.recomputed();
+  return LBM_OK;
+}
+
+}  // extern "C"

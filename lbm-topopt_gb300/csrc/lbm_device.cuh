@@ -1,0 +1,1047 @@
+// lbm_device.cuh -- device-side building blocks of the GB300 LBM kernels:
+// lattices, storage precision traits, collision operators and their
+// transposes, boundary conditions and their transposes, objectives.
+//
+// Populations live in HBM as SoA planes f[q*P + c], c = (z*ny + y)*nx + x
+// (x fastest), one plane per direction, P = padded cell count.  FP64 storage
+// holds f; FP32/FP16 storage holds the deviation f - w_q of the flow
+// populations (temperature populations are stored unshifted), and all
+// formulas then run on the deviation with rho replaced by rho - 1, which is
+// exact for the incompressible equilibrium feq_i = w_i (rho + ...).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lbmgpu.h"
+
+namespace lbm {
+
+enum { LAT_D2Q9 = 0, LAT_D3Q19 = 1, LAT_D2Q9_D2Q5 = 2 };
+
+// ---------------------------------------------------------------------------
+// Lattices (latticeBoltzmann/lattices2d.hh:16-62, lattices3d.hh:141-160).  The
+// thermal lattice appends D2Q5 as directions 9..13.
+
+template <int LAT>
+struct Lattice;
+
+template <>
+struct Lattice<LAT_D2Q9> {
+  static constexpr int Q = 9, QF = 9, HALF = 4, DIM = 2, NMAC = 3;
+  __host__ __device__ static constexpr int ex(int i) {
+    constexpr int v[9] = {0, 1, 0, -1, -1, -1, 0, 1, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ey(int i) {
+    constexpr int v[9] = {0, -1, -1, -1, 0, 1, 1, 1, 0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ez(int) { return 0; }
+  __host__ __device__ static constexpr int opp(int i) {
+    constexpr int v[9] = {0, 5, 6, 7, 8, 1, 2, 3, 4};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double w(int i) {
+    constexpr double v[9] = {4. / 9., 1. / 36., 1. / 9., 1. / 36., 1. / 9.,
+                             1. / 36., 1. / 9., 1. / 36., 1. / 9.};
+    return v[i];
+  }
+};
+
+template <>
+struct Lattice<LAT_D3Q19> {
+  static constexpr int Q = 19, QF = 19, HALF = 9, DIM = 3, NMAC = 4;
+  __host__ __device__ static constexpr int ex(int i) {
+    constexpr int v[19] = {0, 0, 0, -1, 0, 0, -1, 1, -1, 1, 0, 0, 1, 0, 0, 1, -1, 1, -1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ey(int i) {
+    constexpr int v[19] = {0, 0, -1, 0, -1, 1, 0, 0, -1, -1, 0, 1, 0, 1, -1, 0, 0, 1, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ez(int i) {
+    constexpr int v[19] = {0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 1, 0, 0, 1, 1, 1, 1, 0, 0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int opp(int i) {
+    constexpr int v[19] = {0, 10, 11, 12, 13, 14, 15, 16, 17, 18, 1, 2, 3, 4, 5, 6, 7, 8, 9};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double w(int i) {
+    constexpr double v[19] = {1. / 3.,  1. / 18., 1. / 18., 1. / 18., 1. / 36., 1. / 36., 1. / 36.,
+                              1. / 36., 1. / 36., 1. / 36., 1. / 18., 1. / 18., 1. / 18., 1. / 36.,
+                              1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
+    return v[i];
+  }
+};
+
+template <>
+struct Lattice<LAT_D2Q9_D2Q5> {
+  static constexpr int Q = 14, QF = 9, HALF = 4, DIM = 2, NMAC = 4;
+  __host__ __device__ static constexpr int ex(int i) {
+    constexpr int v[14] = {0, 1, 0, -1, -1, -1, 0, 1, 1, 0, 0, -1, 0, 1};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ey(int i) {
+    constexpr int v[14] = {0, -1, -1, -1, 0, 1, 1, 1, 0, 0, -1, 0, 1, 0};
+    return v[i];
+  }
+  __host__ __device__ static constexpr int ez(int) { return 0; }
+  __host__ __device__ static constexpr int opp(int i) {
+    constexpr int v[14] = {0, 5, 6, 7, 8, 1, 2, 3, 4, 9, 12, 13, 10, 11};
+    return v[i];
+  }
+  __host__ __device__ static constexpr double w(int i) {
+    constexpr double v[14] = {4. / 9., 1. / 36., 1. / 9., 1. / 36., 1. / 9., 1. / 36., 1. / 9.,
+                              1. / 36., 1. / 9., 1. / 3., 1. / 6., 1. / 6., 1. / 6., 1. / 6.};
+    return v[i];
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Storage precision.
+
+template <class S>
+struct Store;
+
+template <>
+struct Store<double> {
+  using C = double;   // compute type
+  static constexpr bool SHIFT = false;
+  __device__ static C ld(const double* p) { return *p; }
+  __device__ static void st(double* p, C v) { *p = v; }
+};
+
+template <>
+struct Store<float> {
+  using C = float;
+  static constexpr bool SHIFT = true;
+  __device__ static C ld(const float* p) { return __ldcs(p); }
+  __device__ static void st(float* p, C v) { __stcs(p, v); }
+};
+
+template <>
+struct Store<__half> {
+  using C = float;
+  static constexpr bool SHIFT = true;
+  __device__ static C ld(const __half* p) { return __half2float(*p); }
+  __device__ static void st(__half* p, C v) { *p = __float2half_rn(v); }
+};
+
+// Design field storage: FP64 next to FP64 populations, FP32 otherwise.
+template <class S>
+struct GammaT {
+  using T = float;
+};
+template <>
+struct GammaT<double> {
+  using T = double;
+};
+
+// ---------------------------------------------------------------------------
+// Launch parameters.
+
+struct DevBC {
+  int kind, face, profile;
+  int box[6];
+  double value;   // value * (1 + amp sin(2 pi t / period)) at this launch's time t
+};
+
+struct KParams {
+  int nx, ny, nz;
+  long long P;       // plane stride in elements
+  // model
+  double omega;
+  double mrt[8];
+  double pbb_scale, pbb_q;
+  double diff, ramp_q, ramp_ck, heat_rate, heat_T;
+  // boundary conditions of the input state's time step
+  int nbc;
+  int apply_bc;
+  DevBC bc[LBM_MAX_BC];
+  // objective
+  int objective;
+  int eval_obj;
+  double obj_weight, inv_in, inv_out;
+  int obj_in[6], obj_out[6];
+  double* partial;         // per-block partial sums
+  unsigned int* counter;   // last-block-done counter (reset by the last block)
+  double* result;          // J of this step (written by the last block)
+  // buffers
+  const void* fin;
+  void* fout;
+  const void* gamma;
+  const void* lam_in;      // eta_{t+1}
+  void* lam_out;           // eta_t
+  double* sens;
+  int* error_flag;         // set to a non-zero code on a non-finite result
+};
+
+__host__ __device__ inline bool in_box(const int* b, int x, int y, int z) {
+  return x >= b[0] && x <= b[1] && y >= b[2] && y <= b[3] && z >= b[4] && z <= b[5];
+}
+
+// ---------------------------------------------------------------------------
+// Interpolations (core/interpolationFunctions.hh:17-54).
+
+template <class C>
+__device__ __forceinline__ C bp(C s, C q) {
+  return C(1.) - s * (C(1.) + q) / (q + s);
+}
+template <class C>
+__device__ __forceinline__ C bp_diff(C s, C q) {
+  return (-(C(1.) + q) / (q + s) + s * (C(1.) + q) / ((q + s) * (q + s)));
+}
+template <class C>
+__device__ __forceinline__ C ramp(C s, C q, C ck) {
+  return (s * (ck * (C(1.) + q) - C(1.)) + C(1.)) / (ck * (C(1.) + q * s));
+}
+template <class C>
+__device__ __forceinline__ C ramp_diff(C s, C q, C ck) {
+  return (ck * (C(1.) + q) - C(1.)) / (ck * (C(1.) + q * s)) -
+         ((s * (ck * (C(1.) + q) - C(1.)) + C(1.)) * q) / (ck * (C(1.) + q * s) * (C(1.) + q * s));
+}
+
+// ---------------------------------------------------------------------------
+// Macros (incompressible: u = j).  D2Q9 keeps the grouping of
+// IncompressibleMacros2d<D2Q9> (dynamics/isothermalMacros2d.hh:199-208).
+
+template <class C>
+__device__ __forceinline__ void macros_d2q9(const C* f, C& rho, C& jx, C& jy) {
+  C ux = f[1] + f[7] + f[8];
+  C uy = f[5] + f[6] + f[7];
+  rho = ux + uy - f[7] + f[0] + f[2] + f[3] + f[4];
+  ux -= f[3] + f[4] + f[5];
+  uy -= f[1] + f[2] + f[3];
+  jx = ux;
+  jy = uy;
+}
+
+template <int LAT, class C>
+__device__ __forceinline__ void flow_macros(const C* f, C& rho, C& jx, C& jy, C& jz) {
+  using L = Lattice<LAT>;
+  if (L::DIM == 2) {
+    macros_d2q9(f, rho, jx, jy);
+    jz = C(0.);
+  } else {
+    rho = C(0.);
+    jx = C(0.);
+    jy = C(0.);
+    jz = C(0.);
+#pragma unroll
+    for (int i = 0; i < L::QF; ++i) {
+      rho += f[i];
+      if (L::ex(i) == 1) jx += f[i];
+      if (L::ex(i) == -1) jx -= f[i];
+      if (L::ey(i) == 1) jy += f[i];
+      if (L::ey(i) == -1) jy -= f[i];
+      if (L::ez(i) == 1) jz += f[i];
+      if (L::ez(i) == -1) jz -= f[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// MRT moment bases: rows of the non-conserved moments.
+// D2Q9: dynamics/incompressibleMRT2d.hh:50-60.  D3Q19: dynamics/MRT3d.hh:50-90.
+
+__host__ __device__ constexpr int mrt2d_m(int k, int i) {
+  constexpr int M[6][9] = {{-4, 2, -1, 2, -1, 2, -1, 2, -1}, {4, 1, -2, 1, -2, 1, -2, 1, -2},
+                           {0, 1, 0, -1, 2, -1, 0, 1, -2},   {0, -1, 2, -1, 0, 1, -2, 1, 0},
+                           {0, 0, -1, 0, 1, 0, -1, 0, 1},    {0, -1, 0, 1, 0, -1, 0, 1, 0}};
+  return M[k][i];
+}
+__host__ __device__ constexpr int mrt2d_n(int k) {
+  constexpr int N[6] = {36, 36, 12, 12, 4, 4};
+  return N[k];
+}
+
+__host__ __device__ constexpr int mrt3d_m(int k, int i) {
+  constexpr int M[15][19] = {
+      {-30, -11, -11, -11, 8, 8, 8, 8, 8, 8, -11, -11, -11, 8, 8, 8, 8, 8, 8},
+      {12, -4, -4, -4, 1, 1, 1, 1, 1, 1, -4, -4, -4, 1, 1, 1, 1, 1, 1},
+      {0, 0, 0, 4, 0, 0, -1, 1, -1, 1, 0, 0, -4, 0, 0, 1, -1, 1, -1},
+      {0, 0, 4, 0, -1, 1, 0, 0, -1, -1, 0, -4, 0, 1, -1, 0, 0, 1, 1},
+      {0, 4, 0, 0, -1, -1, -1, -1, 0, 0, -4, 0, 0, 1, 1, 1, 1, 0, 0},
+      {0, -1, -1, 2, -2, -2, 1, 1, 1, 1, -1, -1, 2, -2, -2, 1, 1, 1, 1},
+      {0, 2, 2, -4, -2, -2, 1, 1, 1, 1, 2, 2, -4, -2, -2, 1, 1, 1, 1},
+      {0, -1, 1, 0, 0, 0, -1, -1, 1, 1, -1, 1, 0, 0, 0, -1, -1, 1, 1},
+      {0, 2, -2, 0, 0, 0, -1, -1, 1, 1, 2, -2, 0, 0, 0, -1, -1, 1, 1},
+      {0, 0, 0, 0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 0, 0, 0, 1, -1},
+      {0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0},
+      {0, 0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 0, 0, 0, 1, -1, 0, 0},
+      {0, 0, 0, 0, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 0, -1, 1, 1, -1},
+      {0, 0, 0, 0, -1, 1, 0, 0, 1, 1, 0, 0, 0, 1, -1, 0, 0, -1, -1},
+      {0, 0, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 0, -1, -1, 1, 1, 0, 0}};
+  return M[k][i];
+}
+__host__ __device__ constexpr int mrt3d_n(int k) {
+  constexpr int N[15] = {2394, 252, 40, 40, 40, 36, 72, 12, 24, 4, 4, 4, 8, 8, 8};
+  return N[k];
+}
+
+template <int DIM>
+struct MRT {
+  static constexpr int K = (DIM == 2) ? 6 : 15;
+  static constexpr int QF = (DIM == 2) ? 9 : 19;
+  __host__ __device__ static constexpr int m(int k, int i) {
+    return DIM == 2 ? mrt2d_m(k, i) : mrt3d_m(k, i);
+  }
+  __host__ __device__ static constexpr int n(int k) { return DIM == 2 ? mrt2d_n(k) : mrt3d_n(k); }
+};
+
+// sum_i M[k][i] f_i, left to right, skipping zeros (folds to adds with the
+// constant row).
+template <int DIM, class C>
+__device__ __forceinline__ C mrt_moment(int k, const C* f) {
+  using M = MRT<DIM>;
+  C s = C(0.);
+  bool first = true;
+#pragma unroll
+  for (int i = 0; i < M::QF; ++i) {
+    const int c = M::m(k, i);
+    if (c == 0) continue;
+    if (first) {
+      s = (c == 1) ? f[i] : (c == -1) ? -f[i] : C(c) * f[i];
+      first = false;
+    } else if (c == 1) {
+      s = s + f[i];
+    } else if (c == -1) {
+      s = s - f[i];
+    } else {
+      s = s + C(c) * f[i];
+    }
+  }
+  return s;
+}
+
+// Relaxation r_k = s_k (m_k - meq_k) written as the reference does
+// (incompressibleMRT2d.hh:62-67, MRT3d.hh:92-109).  rho is the "rho-like"
+// value (rho, or rho - 1 for shifted storage).
+template <class C>
+__device__ __forceinline__ void mrt2d_relax(C* mo, C rho, C jx, C jy, const KParams& p) {
+  const C s1 = C(p.mrt[0]), s2 = C(p.mrt[1]), s46 = C(p.mrt[2]), om = C(p.omega);
+  C uSqr = jx * jx + jy * jy;
+  mo[0] = s1 * (mo[0] + C(2.) * rho - C(3.) * uSqr);
+  mo[1] = s2 * (mo[1] - rho + C(3.) * uSqr);
+  mo[2] = s46 * (mo[2] + jx);
+  mo[3] = s46 * (mo[3] + jy);
+  mo[4] = om * (mo[4] - jx * jx + jy * jy);
+  mo[5] = om * (mo[5] - jx * jy);
+}
+
+template <class C>
+__device__ __forceinline__ void mrt3d_relax(C* mo, C rho, C jx, C jy, C jz, const KParams& p) {
+  const C s1 = C(p.mrt[0]), s2 = C(p.mrt[1]), s4 = C(p.mrt[2]), s10 = C(p.mrt[3]),
+          s16 = C(p.mrt[4]), we = C(p.mrt[5]), wej = C(p.mrt[6]), wxx = C(p.mrt[7]),
+          om = C(p.omega);
+  C jSqr = jx * jx + jy * jy + jz * jz;
+  mo[0] = s1 * (mo[0] + C(11.) * rho - C(19.) * jSqr);
+  mo[1] = s2 * (mo[1] - we * rho - wej * jSqr);
+  mo[2] = s4 * (mo[2] + C(2. / 3.) * jx);
+  mo[3] = s4 * (mo[3] + C(2. / 3.) * jy);
+  mo[4] = s4 * (mo[4] + C(2. / 3.) * jz);
+  C tempEq = (C(2.) * jx * jx - (jy * jy + jz * jz));
+  mo[5] = om * (mo[5] - tempEq);
+  mo[6] = s10 * (mo[6] - wxx * tempEq);
+  tempEq = (jy * jy - jz * jz);
+  mo[7] = om * (mo[7] - tempEq);
+  mo[8] = s10 * (mo[8] - wxx * tempEq);
+  mo[9] = om * (mo[9] - jx * jy);
+  mo[10] = om * (mo[10] - jy * jz);
+  mo[11] = om * (mo[11] - jx * jz);
+  mo[12] *= s16;
+  mo[13] *= s16;
+  mo[14] *= s16;
+}
+
+// f_out_i = f_i - sum_k (M[k][i]/N_k) r_k, in k order.
+template <int DIM, class C>
+__device__ __forceinline__ void mrt_backmap(C* f, const C* mo) {
+  using M = MRT<DIM>;
+#pragma unroll
+  for (int i = 0; i < M::QF; ++i) {
+    C v = f[i];
+#pragma unroll
+    for (int k = 0; k < M::K; ++k) {
+      const int c = M::m(k, i);
+      if (c == 0) continue;
+      v = v + C(-(double)c / (double)M::n(k)) * mo[k];
+    }
+    f[i] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forward flow collision in place: f <- PBB(base(f)); returns the macros of
+// the input.  IncompressibleBGK2d<D2Q9> (dynamics/incompressibleBGK2d.hh:120-147),
+// incompressible BGK on D3Q19 (dynamics/BGK3d.hh), IncompressibleMRT2d/3d,
+// PartialBouncebackCollision (dynamics/partialBouncebackCollision.hh:53-65).
+
+template <int LAT, int COLL, class C>
+__device__ __forceinline__ void flow_collide(C* f, C imult, C& rho, C& jx, C& jy, C& jz,
+                                             const KParams& p) {
+  using L = Lattice<LAT>;
+  flow_macros<LAT>(f, rho, jx, jy, jz);
+  const C om = C(p.omega);
+  if (COLL == LBM_BGK) {
+    if (L::DIM == 2) {
+      const C uSqr = jx * jx + jy * jy;
+      const C cFeq = rho - C(1.5) * uSqr;
+      const C rel = C(1.) - om;
+      const C restW = C(4. / 9.), stW = C(1. / 9.), diagW = C(1. / 36.);
+      f[0] = rel * f[0] + om * restW * cFeq;
+      f[2] = rel * f[2] + om * stW * (cFeq - C(3.) * jy + C(4.5) * jy * jy);
+      f[4] = rel * f[4] + om * stW * (cFeq - C(3.) * jx + C(4.5) * jx * jx);
+      f[6] = rel * f[6] + om * stW * (cFeq + C(3.) * jy + C(4.5) * jy * jy);
+      f[8] = rel * f[8] + om * stW * (cFeq + C(3.) * jx + C(4.5) * jx * jx);
+      f[1] = rel * f[1] + om * diagW * (cFeq + C(3.) * (jx - jy) + C(4.5) * (uSqr - C(2.) * jx * jy));
+      f[3] = rel * f[3] + om * diagW * (cFeq - C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
+      f[5] = rel * f[5] + om * diagW * (cFeq + C(3.) * (jy - jx) + C(4.5) * (uSqr - C(2.) * jx * jy));
+      f[7] = rel * f[7] + om * diagW * (cFeq + C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
+    } else {
+      const C uSqr = jx * jx + jy * jy + jz * jz;
+#pragma unroll
+      for (int i = 0; i < L::QF; ++i) {
+        C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+        C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
+        f[i] = f[i] * (C(1.) - om) + om * eq;
+      }
+    }
+  } else {
+    C mo[MRT<L::DIM>::K];
+#pragma unroll
+    for (int k = 0; k < MRT<L::DIM>::K; ++k) mo[k] = mrt_moment<L::DIM>(k, f);
+    if (L::DIM == 2)
+      mrt2d_relax(mo, rho, jx, jy, p);
+    else
+      mrt3d_relax(mo, rho, jx, jy, jz, p);
+    mrt_backmap<L::DIM>(f, mo);
+  }
+#pragma unroll
+  for (int d = 1; d <= L::HALF; ++d) {
+    C ftemp = f[d];
+    f[d] += imult * (f[d + L::HALF] - f[d]);
+    f[d + L::HALF] += imult * (ftemp - f[d + L::HALF]);
+  }
+}
+
+// Transpose of flow_collide: on entry lam = adjoint of the output, on exit
+// lam = adjoint of the input; dg += d(out)/d(imult)^T lam * dimult.
+// ReversePartialBouncebackCollision (adjointDynamics/reversePartialBounceback.hh:18-41)
+// over ReverseIncompressibleBGK2d<D2Q9> (reverseIncompressibleBGK2d.hh:112-169)
+// and the transposes of the MRT operators (derived from the forward).
+template <int LAT, int COLL, class C>
+__device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C dimult, C& dg,
+                                             const KParams& p) {
+  using L = Lattice<LAT>;
+  constexpr int QF = L::QF;
+  C fo[QF];
+#pragma unroll
+  for (int i = 0; i < QF; ++i) fo[i] = fin[i];
+  C rho, jx, jy, jz;
+  {
+    // base collision output (without PBB), as the reverse PBB recomputes it
+    flow_macros<LAT>(fo, rho, jx, jy, jz);
+    const C om = C(p.omega);
+    if (COLL == LBM_BGK) {
+      if (L::DIM == 2) {
+        const C uSqr = jx * jx + jy * jy;
+        const C cFeq = rho - C(1.5) * uSqr;
+        const C rel = C(1.) - om;
+        const C restW = C(4. / 9.), stW = C(1. / 9.), diagW = C(1. / 36.);
+        fo[0] = rel * fo[0] + om * restW * cFeq;
+        fo[2] = rel * fo[2] + om * stW * (cFeq - C(3.) * jy + C(4.5) * jy * jy);
+        fo[4] = rel * fo[4] + om * stW * (cFeq - C(3.) * jx + C(4.5) * jx * jx);
+        fo[6] = rel * fo[6] + om * stW * (cFeq + C(3.) * jy + C(4.5) * jy * jy);
+        fo[8] = rel * fo[8] + om * stW * (cFeq + C(3.) * jx + C(4.5) * jx * jx);
+        fo[1] = rel * fo[1] + om * diagW * (cFeq + C(3.) * (jx - jy) + C(4.5) * (uSqr - C(2.) * jx * jy));
+        fo[3] = rel * fo[3] + om * diagW * (cFeq - C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
+        fo[5] = rel * fo[5] + om * diagW * (cFeq + C(3.) * (jy - jx) + C(4.5) * (uSqr - C(2.) * jx * jy));
+        fo[7] = rel * fo[7] + om * diagW * (cFeq + C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
+      } else {
+        const C uSqr = jx * jx + jy * jy + jz * jz;
+#pragma unroll
+        for (int i = 0; i < QF; ++i) {
+          C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+          C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
+          fo[i] = fo[i] * (C(1.) - om) + om * eq;
+        }
+      }
+    } else {
+      C mo[MRT<L::DIM>::K];
+#pragma unroll
+      for (int k = 0; k < MRT<L::DIM>::K; ++k) mo[k] = mrt_moment<L::DIM>(k, fo);
+      if (L::DIM == 2)
+        mrt2d_relax(mo, rho, jx, jy, p);
+      else
+        mrt3d_relax(mo, rho, jx, jy, jz, p);
+      mrt_backmap<L::DIM>(fo, mo);
+    }
+  }
+  // reverse PBB
+  C imultRev = C(0.);
+#pragma unroll
+  for (int d = 1; d <= L::HALF; ++d) {
+    imultRev += (fo[d] - fo[d + L::HALF]) * lam[d + L::HALF];
+    imultRev += (fo[d + L::HALF] - fo[d]) * lam[d];
+    C t = lam[d + L::HALF];
+    lam[d + L::HALF] += imult * (lam[d] - lam[d + L::HALF]);
+    lam[d] += imult * (t - lam[d]);
+  }
+  dg += dimult * imultRev;
+  // reverse base collision
+  const C om = C(p.omega);
+  if (COLL == LBM_BGK) {
+    if (L::DIM == 2) {
+      const C rel = C(1.) - om;
+      const C restW = C(4. / 9.), stW = C(1. / 9.), diagW = C(1. / 36.);
+      C r0 = C(0.), r1 = C(0.), r2 = C(0.);
+      C uSqrRev, cFeqRev, temp;
+      C li[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) li[i] = rel * lam[i];
+      temp = om * diagW * lam[7];
+      cFeqRev = temp;
+      uSqrRev = temp;
+      r1 += temp * (C(9.) * jy + C(3.));
+      r2 += C(3.) * temp * (C(3.) * jx + C(1.));
+      temp = om * diagW * lam[5];
+      cFeqRev += temp;
+      uSqrRev += temp;
+      r1 -= temp * (C(9.) * jy + C(3.));
+      r2 += temp * (C(3.) - C(9.) * jx);
+      temp = om * diagW * lam[3];
+      cFeqRev += temp;
+      uSqrRev += temp;
+      r1 += temp * (C(9.) * jy - C(3.));
+      r2 += temp * (C(9.) * jx - C(3.));
+      temp = om * diagW * lam[1];
+      cFeqRev += temp;
+      uSqrRev += temp;
+      uSqrRev *= C(4.5);
+      r1 += temp * (C(3.) - C(9.) * jy);
+      r2 -= temp * (C(9.) * jx + C(3.));
+      temp = om * stW * lam[8];
+      cFeqRev += temp;
+      r1 += (C(9.) * jx + C(3.)) * temp;
+      temp = om * stW * lam[6];
+      cFeqRev += temp;
+      r2 = r2 + (C(9.) * jy + C(3.)) * temp;
+      temp = om * stW * lam[4];
+      cFeqRev += temp;
+      r1 = r1 + (C(9.) * jx - C(3.)) * temp;
+      temp = om * stW * lam[2];
+      cFeqRev += temp + om * restW * lam[0];
+      r2 = r2 + (C(9.) * jy - C(3.)) * temp;
+      uSqrRev -= C(1.5) * cFeqRev;
+      r0 = r0 + cFeqRev;
+      r1 = r1 + C(2.) * jx * uSqrRev;
+      r2 = r2 + C(2.) * jy * uSqrRev;
+      lam[0] = li[0] + r0;
+      lam[1] = li[1] + (r0 + r1 - r2);
+      lam[2] = li[2] + (r0 - r2);
+      lam[3] = li[3] + (r0 - r1 - r2);
+      lam[4] = li[4] + (r0 - r1);
+      lam[5] = li[5] + (r0 - r1 + r2);
+      lam[6] = li[6] + (r0 + r2);
+      lam[7] = li[7] + (r0 + r1 + r2);
+      lam[8] = li[8] + (r0 + r1);
+    } else {
+      C rR = C(0.), jR0 = C(0.), jR1 = C(0.), jR2 = C(0.);
+#pragma unroll
+      for (int i = 0; i < QF; ++i) {
+        C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+        C a = om * C(L::w(i)) * lam[i];
+        rR += a;
+        C ds = a * (C(3.) + C(9.) * sc);
+        jR0 += ds * C(L::ex(i)) - C(3.) * a * jx;
+        jR1 += ds * C(L::ey(i)) - C(3.) * a * jy;
+        jR2 += ds * C(L::ez(i)) - C(3.) * a * jz;
+      }
+#pragma unroll
+      for (int i = 0; i < QF; ++i)
+        lam[i] = (C(1.) - om) * lam[i] + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) +
+                                          jR2 * C(L::ez(i)));
+    }
+  } else {
+    using M = MRT<L::DIM>;
+    C a[M::K];
+    C rate[M::K];
+    if (L::DIM == 2) {
+      rate[0] = C(p.mrt[0]);
+      rate[1] = C(p.mrt[1]);
+      rate[2] = C(p.mrt[2]);
+      rate[3] = C(p.mrt[2]);
+      rate[4] = om;
+      rate[5] = om;
+    } else {
+      rate[0] = C(p.mrt[0]);
+      rate[1] = C(p.mrt[1]);
+      rate[2] = rate[3] = rate[4] = C(p.mrt[2]);
+      rate[5] = om;
+      rate[6] = C(p.mrt[3]);
+      rate[7] = om;
+      rate[8] = C(p.mrt[3]);
+      rate[9] = rate[10] = rate[11] = om;
+      rate[12] = rate[13] = rate[14] = C(p.mrt[4]);
+    }
+#pragma unroll
+    for (int k = 0; k < M::K; ++k) {
+      // sum_i (-M[k][i]/N_k) lam_i
+      C s = mrt_moment<L::DIM>(k, lam);
+      a[k] = rate[k] * (C(-1.0 / (double)M::n(k)) * s);
+    }
+    C rR, jR0, jR1, jR2;
+    if (L::DIM == 2) {
+      rR = -(a[0] * C(-2.) + a[1]);
+      jR0 = -(a[0] * C(6.) * jx - a[1] * C(6.) * jx - a[2] + a[4] * C(2.) * jx + a[5] * jy);
+      jR1 = -(a[0] * C(6.) * jy - a[1] * C(6.) * jy - a[3] - a[4] * C(2.) * jy + a[5] * jx);
+      jR2 = C(0.);
+    } else {
+      const C we = C(p.mrt[5]), wej = C(p.mrt[6]), wxx = C(p.mrt[7]);
+      const C c2 = C(-2. / 3.);
+      const C a56 = a[5] + wxx * a[6], a78 = a[7] + wxx * a[8];
+      rR = -(a[0] * C(-11.) + a[1] * we);
+      jR0 = -(a[0] * C(38.) * jx + a[1] * C(2.) * wej * jx + a[2] * c2 + a56 * C(4.) * jx +
+              a[9] * jy + a[11] * jz);
+      jR1 = -(a[0] * C(38.) * jy + a[1] * C(2.) * wej * jy + a[3] * c2 - a56 * C(2.) * jy +
+              a78 * C(2.) * jy + a[9] * jx + a[10] * jz);
+      jR2 = -(a[0] * C(38.) * jz + a[1] * C(2.) * wej * jz + a[4] * c2 - a56 * C(2.) * jz -
+              a78 * C(2.) * jz + a[10] * jy + a[11] * jx);
+    }
+#pragma unroll
+    for (int i = 0; i < QF; ++i) {
+      C v = lam[i];
+#pragma unroll
+      for (int k = 0; k < M::K; ++k) {
+        const int c = M::m(k, i);
+        if (c == 0) continue;
+        v += C(c) * a[k];
+      }
+      lam[i] = v + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) + jR2 * C(L::ez(i)));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Temperature lattice (D2Q5, directions 9..13): ThermalBGK2d with the obstacle
+// rate of ThermalObstacleCollision (dynamics/thermalBGK2d.hh:58-65,
+// thermalObstacleCollision.hh:47-53) after the flow collision
+// (thermalDualCollision.hh:57-64), plus solid heating (1-g) h (Th - T) w_i.
+
+template <class C>
+__device__ __forceinline__ C thermal_omega(C g, const KParams& p) {
+  C imult = C(p.diff) * ramp(g, C(p.ramp_q), C(p.ramp_ck));
+  return C(1.) / (C(3.) * imult + C(0.5));
+}
+
+template <class C>
+__device__ __forceinline__ void thermal_collide(C* gp, C ux, C uy, C g, C& T, const KParams& p) {
+  constexpr double W5[5] = {1. / 3., 1. / 6., 1. / 6., 1. / 6., 1. / 6.};
+  constexpr int EX5[5] = {0, 0, -1, 0, 1}, EY5[5] = {0, -1, 0, 1, 0};
+  const C om = thermal_omega(g, p);
+  T = gp[0] + gp[1] + gp[2] + gp[3] + gp[4];
+  const C hs = (C(1.) - g) * C(p.heat_rate) * (C(p.heat_T) - T);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    C sc = C(EX5[i]) * ux + C(EY5[i]) * uy;
+    C eq = C(W5[i]) * T * (C(1.) + C(3.) * sc);
+    gp[i] = gp[i] * (C(1.) - om) + om * eq;
+    gp[i] += C(W5[i]) * hs;
+  }
+}
+
+// Transpose of thermal_collide at input (gin, ux, uy); lam[0..4] in/out;
+// returns the adjoint of (ux, uy) and adds to dg.
+template <class C>
+__device__ __forceinline__ void thermal_reverse(const C* gin, C* lam, C ux, C uy, C g, C& uxR,
+                                                C& uyR, C& dg, const KParams& p) {
+  constexpr double W5[5] = {1. / 3., 1. / 6., 1. / 6., 1. / 6., 1. / 6.};
+  constexpr int EX5[5] = {0, 0, -1, 0, 1}, EY5[5] = {0, -1, 0, 1, 0};
+  const C T = gin[0] + gin[1] + gin[2] + gin[3] + gin[4];
+  const C om = thermal_omega(g, p);
+  C TR = C(0.), omR = C(0.), hsR = C(0.);
+  uxR = C(0.);
+  uyR = C(0.);
+  C li[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    C sc = C(EX5[i]) * ux + C(EY5[i]) * uy;
+    C eq = C(W5[i]) * T * (C(1.) + C(3.) * sc);
+    li[i] = (C(1.) - om) * lam[i];
+    omR += (eq - gin[i]) * lam[i];
+    C a = om * lam[i] * C(W5[i]);
+    TR += a * (C(1.) + C(3.) * sc);
+    uxR += a * T * C(3.) * C(EX5[i]);
+    uyR += a * T * C(3.) * C(EY5[i]);
+    hsR += C(W5[i]) * lam[i];
+  }
+  TR += -(C(1.) - g) * C(p.heat_rate) * hsR;
+  dg += -C(p.heat_rate) * (C(p.heat_T) - T) * hsR;
+  const C den = C(3.) * C(p.diff) * ramp(g, C(p.ramp_q), C(p.ramp_ck)) + C(0.5);
+  dg += omR * (C(-1.) / (den * den)) * C(3.) * C(p.diff) * ramp_diff(g, C(p.ramp_q), C(p.ramp_ck));
+#pragma unroll
+  for (int i = 0; i < 5; ++i) lam[i] = li[i] + TR;
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions on one cell's post-stream populations at time t.
+// Zou-He (boundaryConditions/ZouHe2d.hh:23-281), Hecht (Hecht3d.hh:62-94,175-209),
+// thermal Zou-He (thermalZouHe2d.hh:63-81).
+
+__device__ __forceinline__ double bc_profile(const DevBC& b, int y, int z, int ny, int nz, int dim) {
+  if (b.profile != LBM_PROFILE_PARABOLIC) return 1.;
+  double mid = (double)(ny - 1) / 2.;
+  double pr = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
+  if (dim == 3) {
+    double mz = (double)(nz - 1) / 2.;
+    pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
+  }
+  return pr;
+}
+
+template <int LAT, bool SHIFT, class C>
+__device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KParams& p) {
+  using L = Lattice<LAT>;
+  for (int k = 0; k < p.nbc; ++k) {
+    const DevBC& b = p.bc[k];
+    if (!in_box(b.box, x, y, z)) continue;
+    if (b.kind == LBM_BC_VELOCITY) {
+      double vv = b.value;
+      vv *= bc_profile(b, y, z, p.ny, p.nz, L::DIM);
+      const C ux = C(vv);
+      if (L::DIM == 2) {
+        const C uy = C(0.);
+        if (b.face == LBM_FACE_WEST) {
+          f[1] = C(0.5) * (f[6] - f[2]) + f[5] + C(1. / 6.) * ux - C(0.5) * uy;
+          f[7] = C(0.5) * (f[2] - f[6]) + f[3] + C(1. / 6.) * ux + C(0.5) * uy;
+          f[8] = f[4] + C(2. / 3.) * ux;
+        } else if (b.face == LBM_FACE_EAST) {
+          f[3] = f[7] + C(0.5) * (f[6] - f[2]) - C(1. / 6.) * ux - C(0.5) * uy;
+          f[4] = f[8] - C(2. / 3.) * ux;
+          f[5] = f[1] + C(0.5) * (f[2] - f[6]) - C(1. / 6.) * ux + C(0.5) * uy;
+        }
+      } else {
+        const C uy = C(0.), uz = C(0.);
+        if (b.face == LBM_FACE_WEST) {
+          C Nyx = C(0.5) * (f[5] + f[11] + f[13] - (f[2] + f[4] + f[14])) - C(1. / 3.) * uy;
+          C Nzx = C(0.5) * (f[10] + f[13] + f[14] - (f[1] + f[4] + f[5])) - C(1. / 3.) * uz;
+          f[7] = f[16] + C(1. / 6.) * (ux - uz) + Nzx;
+          f[9] = f[18] + C(1. / 6.) * (ux - uy) + Nyx;
+          f[12] = f[3] + C(1. / 3.) * ux;
+          f[15] = f[6] + C(1. / 6.) * (ux + uz) - Nzx;
+          f[17] = f[8] + C(1. / 6.) * (ux + uy) - Nyx;
+        }
+      }
+    } else if (b.kind == LBM_BC_PRESSURE) {
+      const C rho0 = SHIFT ? C(b.value - 1.) : C(b.value);
+      if (L::DIM == 2) {
+        if (b.face == LBM_FACE_EAST) {
+          C ux0 = -rho0 + (f[0] + f[2] + f[6] + C(2.) * (f[1] + f[7] + f[8]));
+          f[4] = f[8] - C(2. / 3.) * ux0;
+          f[3] = f[7] - C(1. / 6.) * ux0 + C(0.5) * (f[6] - f[2]);
+          f[5] = f[1] - C(1. / 6.) * ux0 + C(0.5) * (f[2] - f[6]);
+        } else if (b.face == LBM_FACE_WEST) {
+          C ux0 = rho0 - (f[0] + f[2] + f[6] + C(2.) * (f[3] + f[4] + f[5]));
+          f[8] = f[4] + C(2. / 3.) * ux0;
+          f[7] = f[3] + C(1. / 6.) * ux0 + C(0.5) * (f[2] - f[6]);
+          f[1] = f[5] + C(1. / 6.) * ux0 + C(0.5) * (f[6] - f[2]);
+        }
+      } else if (b.face == LBM_FACE_EAST) {
+        C ux = f[0] + f[1] + f[2] + f[4] + f[5] + f[10] + f[11] + f[13] + f[14] +
+               C(2.) * (f[7] + f[9] + f[12] + f[15] + f[17]) - rho0;
+        C Nyx = C(0.5) * (f[5] + f[11] + f[13] - (f[2] + f[4] + f[14]));
+        C Nzx = C(0.5) * (f[10] + f[13] + f[14] - (f[1] + f[4] + f[5]));
+        f[3] = f[12] - C(1. / 3.) * ux;
+        f[6] = f[15] - C(1. / 6.) * ux + Nzx;
+        f[8] = f[17] - C(1. / 6.) * ux + Nyx;
+        f[16] = f[7] - C(1. / 6.) * ux - Nzx;
+        f[18] = f[9] - C(1. / 6.) * ux - Nyx;
+      }
+    } else if (b.kind == LBM_BC_TEMPERATURE && LAT == LAT_D2Q9_D2Q5) {
+      if (b.face == LBM_FACE_WEST) {
+        C* g = f + 9;
+        g[4] = C(b.value) - g[0] - g[1] - g[2] - g[3];
+      }
+    }
+  }
+}
+
+// Transposes, applied in reverse order of the forward boundary loops
+// (adjointBoundaryConditions/adjointZouHe2d.cc:5-112, adjointHecht3d.cc:7-80).
+template <int LAT, class C>
+__device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KParams& p) {
+  using L = Lattice<LAT>;
+  for (int k = p.nbc - 1; k >= 0; --k) {
+    const DevBC& b = p.bc[k];
+    if (!in_box(b.box, x, y, z)) continue;
+    if (L::DIM == 3) {
+      if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) {
+        a[1] += C(0.5) * (a[15] - a[7]);
+        a[2] += C(0.5) * (a[17] - a[9]);
+        a[3] += a[12];
+        a[4] += C(0.5) * (a[15] + a[17] - (a[7] + a[9]));
+        a[5] += C(0.5) * (a[9] + a[15] - (a[7] + a[17]));
+        a[6] += a[15];
+        a[8] += a[17];
+        a[10] += C(0.5) * (a[7] - a[15]);
+        a[11] += C(0.5) * (a[9] - a[17]);
+        a[13] += C(0.5) * (a[7] + a[9] - (a[15] + a[17]));
+        a[14] += C(0.5) * (a[7] + a[17] - (a[9] + a[15]));
+        a[16] += a[7];
+        a[18] += a[9];
+        a[7] = a[9] = a[12] = a[15] = a[17] = C(0.);
+      } else if (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_EAST) {
+        C adjUx = -C(1. / 3.) * a[3] - C(1. / 6.) * (a[6] + a[8] + a[16] + a[18]);
+        a[0] += adjUx;
+        a[1] += adjUx + C(0.5) * (a[16] - a[6]);
+        a[2] += adjUx + C(0.5) * (a[18] - a[8]);
+        a[4] += adjUx + C(0.5) * (a[16] + a[18] - (a[6] + a[8]));
+        a[5] += adjUx + C(0.5) * (a[8] + a[16] - (a[6] + a[18]));
+        a[7] += C(2.) * adjUx + a[16];
+        a[9] += C(2.) * adjUx + a[18];
+        a[10] += adjUx + C(0.5) * (a[6] - a[16]);
+        a[11] += adjUx + C(0.5) * (a[8] - a[18]);
+        a[12] += C(2.) * adjUx + a[3];
+        a[13] += adjUx + C(0.5) * (a[6] + a[8] - (a[16] + a[18]));
+        a[14] += adjUx + C(0.5) * (a[6] + a[18] - (a[8] + a[16]));
+        a[15] += C(2.) * adjUx + a[6];
+        a[17] += C(2.) * adjUx + a[8];
+        a[3] = a[6] = a[8] = a[16] = a[18] = C(0.);
+      }
+      continue;
+    }
+    if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) {
+      a[2] += C(0.5) * (a[7] - a[1]);
+      a[3] += a[7];
+      a[4] += a[8];
+      a[5] += a[1];
+      a[6] += C(0.5) * (a[1] - a[7]);
+      a[1] = a[7] = a[8] = C(0.);
+    } else if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_EAST) {
+      a[1] += a[5];
+      a[2] += C(0.5) * (a[5] - a[3]);
+      a[6] += C(0.5) * (a[3] - a[5]);
+      a[7] += a[3];
+      a[8] += a[4];
+      a[3] = a[4] = a[5] = C(0.);
+    } else if (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_EAST) {
+      C adjU = -C(1. / 6.) * a[3] - C(2. / 3.) * a[4] - C(1. / 6.) * a[5];
+      a[0] += adjU;
+      a[1] += C(2.) * adjU + a[5];
+      a[2] += adjU + C(0.5) * (a[5] - a[3]);
+      a[6] += adjU + C(0.5) * (a[3] - a[5]);
+      a[7] += C(2.) * adjU + a[3];
+      a[8] += C(2.) * adjU + a[4];
+      a[3] = a[4] = a[5] = C(0.);
+    } else if (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_WEST) {
+      C adjU = C(1. / 6.) * a[1] + C(1. / 6.) * a[7] + C(2. / 3.) * a[8];
+      a[0] -= adjU;
+      a[2] -= adjU - C(0.5) * (a[7] - a[1]);
+      a[3] -= C(2.) * adjU - a[7];
+      a[4] -= C(2.) * adjU - a[8];
+      a[5] -= C(2.) * adjU - a[1];
+      a[6] -= adjU - C(0.5) * (a[1] - a[7]);
+      a[1] = a[7] = a[8] = C(0.);
+    } else if (b.kind == LBM_BC_TEMPERATURE && b.face == LBM_FACE_WEST && LAT == LAT_D2Q9_D2Q5) {
+      C* g = a + 9;
+      g[0] -= g[4];
+      g[1] -= g[4];
+      g[2] -= g[4];
+      g[3] -= g[4];
+      g[4] = C(0.);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Objectives of one cell (value) and their partial derivatives.
+// PressureDrop2d (functionals/pressureDrop2d.hh:30-68), ThermalOutflowEast2d
+// (temperatureFlow2d.hh:106-142), dissipated power (no reference counterpart):
+// D = 2 alpha |j|^2 + (9/2) nu omega^2 sum_ab Pneq_ab^2.
+
+template <int LAT, bool SHIFT, class C>
+__device__ __forceinline__ double objective_cell(const C* f, C g, int x, int y, int z,
+                                                 const KParams& p) {
+  using L = Lattice<LAT>;
+  if (p.objective == LBM_OBJ_PRESSURE_DROP) {
+    bool i1 = in_box(p.obj_in, x, y, z), i2 = in_box(p.obj_out, x, y, z);
+    if (!i1 && !i2) return 0.;
+    C rho, jx, jy, jz;
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    double r = SHIFT ? 1. + (double)rho : (double)rho;
+    double v = 0.;
+    if (i1) v += p.obj_weight * p.inv_in * r;
+    if (i2) v -= p.obj_weight * p.inv_out * r;
+    return v;
+  }
+  if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
+    if (!in_box(p.obj_out, x, y, z)) return 0.;
+    C rho, jx, jy, jz;
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    C T = f[9] + f[10] + f[11] + f[12] + f[13];
+    return -p.obj_weight * (double)jx * (double)T;
+  }
+  if (p.objective == LBM_OBJ_DISSIPATION) {
+    C rho, j[3];
+    flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
+    C P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
+#pragma unroll
+    for (int i = 0; i < L::QF; ++i) {
+      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
+#pragma unroll
+      for (int a = 0; a < L::DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < L::DIM; ++b)
+          if (e[a] * e[b] != 0) P[a][b] += C(e[a] * e[b]) * f[i];
+    }
+    C s2 = C(0.);
+#pragma unroll
+    for (int a = 0; a < L::DIM; ++a) {
+#pragma unroll
+      for (int b = 0; b < L::DIM; ++b) {
+        C v = P[a][b] - j[a] * j[b];
+        if (a == b) v -= rho / C(3.);
+        s2 += v * v;
+      }
+    }
+    const double om = p.omega, nu = (1. / om - 0.5) / 3.;
+    const C cv = C(4.5 * nu * om * om);
+    const C alpha = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
+    C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    return p.obj_weight * (double)(C(2.) * alpha * jj + cv * s2);
+  }
+  return 0.;
+}
+
+// lam += weight * dF/df ; dg += weight * dF/dgamma
+template <int LAT, bool SHIFT, class C>
+__device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg, int x, int y,
+                                                 int z, const KParams& p) {
+  using L = Lattice<LAT>;
+  if (p.objective == LBM_OBJ_PRESSURE_DROP) {
+    if (in_box(p.obj_in, x, y, z)) {
+      const C v = C(p.inv_in * p.obj_weight);
+#pragma unroll
+      for (int d = 0; d < L::QF; ++d) lam[d] += v;
+    }
+    if (in_box(p.obj_out, x, y, z)) {
+      const C v = C(p.inv_out * p.obj_weight);
+#pragma unroll
+      for (int d = 0; d < L::QF; ++d) lam[d] -= v;
+    }
+  } else if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
+    if (in_box(p.obj_out, x, y, z)) {
+      C rho, jx, jy, jz;
+      flow_macros<LAT>(f, rho, jx, jy, jz);
+      C T = f[9] + f[10] + f[11] + f[12] + f[13];
+      const C tc = C(p.obj_weight);
+#pragma unroll
+      for (int d = 0; d < 9; ++d) lam[d] -= tc * C(L::ex(d)) * T;
+#pragma unroll
+      for (int d = 9; d < 14; ++d) lam[d] -= tc * jx;
+    }
+  } else if (p.objective == LBM_OBJ_DISSIPATION) {
+    C rho, j[3];
+    flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
+    C P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
+#pragma unroll
+    for (int i = 0; i < L::QF; ++i) {
+      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
+#pragma unroll
+      for (int a = 0; a < L::DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < L::DIM; ++b)
+          if (e[a] * e[b] != 0) P[a][b] += C(e[a] * e[b]) * f[i];
+    }
+    C tr = C(0.);
+#pragma unroll
+    for (int a = 0; a < L::DIM; ++a) {
+#pragma unroll
+      for (int b = 0; b < L::DIM; ++b) P[a][b] -= j[a] * j[b];
+      P[a][a] -= rho / C(3.);
+      tr += P[a][a];
+    }
+    const double om = p.omega, nu = (1. / om - 0.5) / 3.;
+    const C cv = C(4.5 * nu * om * om);
+    const C alpha = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
+    const C tc = C(p.obj_weight);
+#pragma unroll
+    for (int i = 0; i < L::QF; ++i) {
+      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
+      C pe = C(0.), pej = C(0.);
+#pragma unroll
+      for (int a = 0; a < L::DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < L::DIM; ++b) {
+          if (e[a] * e[b] != 0) pe += P[a][b] * C(e[a] * e[b]);
+          if (e[a] != 0) pej += P[a][b] * C(e[a]) * j[b];
+        }
+      C ej = C(e[0]) * j[0] + C(e[1]) * j[1] + C(e[2]) * j[2];
+      lam[i] += tc * (C(4.) * alpha * ej + cv * C(2.) * (pe - tr / C(3.) - C(2.) * pej));
+    }
+    C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    dg += tc * (C(2.) * (C(0.5) * (C(p.pbb_scale) * bp_diff(g, C(p.pbb_q)))) * jj);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic block + grid reduction of one double per thread: each block
+// writes its partial, the last block to finish sums the partials in a fixed
+// order and writes *result.
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const int nthr = blockDim.x * blockDim.y;
+  if ((tid & 31) == 0) sh[tid >> 5] = v;
+  __syncthreads();
+  double s = 0.;
+  if (tid < 32) {
+    s = (tid < (nthr + 31) / 32) ? sh[tid] : 0.;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  return s;   // valid in thread 0
+}
+
+__device__ __forceinline__ void grid_reduce(double v, const KParams& p) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  double s = block_sum(v, sh);
+  if (tid == 0) {
+    p.partial[bid] = s;
+    __threadfence();
+    unsigned prev = atomicAdd(p.counter, 1u);
+    last = (prev == nblk - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int nthr = blockDim.x * blockDim.y;
+  double acc = 0.;
+  for (unsigned i = tid; i < nblk; i += nthr) acc += ((volatile double*)p.partial)[i];
+  __syncthreads();
+  double tot = block_sum(acc, sh);
+  if (tid == 0) {
+    *p.result = tot;
+    *p.counter = 0u;
+  }
+}
+
+}  // namespace lbm

@@ -1,0 +1,29 @@
+// lbm_ops.h -- per-lattice kernel launchers (one translation unit per lattice).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace lbm {
+
+struct KParams;
+
+enum {
+  K_FORWARD = 0,
+  K_ADJOINT,
+  K_OBJECTIVE,
+  K_INIT,
+  K_EXPORT,
+  K_IMPORT,
+  K_MACROS,
+  K_EXPORT_ADJ,
+  K_GAMMA,
+};
+
+typedef void (*LaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st, const KParams& p,
+                         double* aux);
+
+LaunchFn launcher_d2q9(int collision, int storage);
+LaunchFn launcher_d3q19(int collision, int storage);
+LaunchFn launcher_thermal(int collision, int storage);
+
+}  // namespace lbm

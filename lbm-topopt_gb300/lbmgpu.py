@@ -34,7 +34,7 @@ LIB_PATH = os.path.join(HERE, "liblbmgpu.so")
 D2Q9, D3Q19, D2Q9_D2Q5 = 0, 1, 2
 BGK, MRT = 0, 1
 STORE_FP64, STORE_FP32, STORE_FP16 = 0, 1, 2
-BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE, BC_THERMAL_NEUMANN = 1, 2, 3, 4
+BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE = 1, 2, 3
 FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
 PROFILE_UNIFORM, PROFILE_PARABOLIC = 0, 1
 OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX = 0, 1, 2, 3

@@ -737,13 +737,6 @@ static void zouhe2d(const model_t* m, const lbm_bc* b, int t, double* F) {
           /* ThermalZouHeWest2d<.,D2Q5,.> (boundaryConditions/thermalZouHe2d.hh:63-81) */
           double* g = f + 9;
           if (b->face == LBM_FACE_WEST) g[4] = v - g[0] - g[1] - g[2] - g[3];
-        } else if (b->kind == LBM_BC_THERMAL_NEUMANN) {
-          /* zero normal gradient: copy the unknown from the inner neighbour */
-          double* g = f + 9;
-          if (b->face == LBM_FACE_EAST) {
-            const double* gn = g - Q;
-            g[2] = gn[2];
-          }
         }
       }
 }
@@ -903,11 +896,6 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             g[2] -= g[4];
             g[3] -= g[4];
             g[4] = 0.;
-          } else if (b->kind == LBM_BC_THERMAL_NEUMANN && b->face == LBM_FACE_EAST) {
-            double* g = a + 9;
-            double* gn = g - Q;
-            gn[2] += g[2];
-            g[2] = 0.;
           }
         }
   }
@@ -1229,6 +1217,17 @@ int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macro
       step(&m, seg + (int64_t)(s - base + 1) * S, tmp, gamma, s);
     }
     for (; t > base; --t) adjoint_step(&m, seg + (int64_t)(t - base) * S, lam, tmp, gamma, sens, t);
+  }
+  /* The collision of f_0 also depends on the design.  The reference's reverse loop
+   * stops at step 1 (applications/RobustPump2d/robustPump2d.cc:268-276) and leaves
+   * this term out; it is exactly zero for the isothermal operators when f_0 is a rest
+   * state, and is added here so the gradient is the derivative of J. */
+  memcpy(seg, ck, sizeof(double) * S);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < m.ncell; ++c) {
+    double li[28], dg = 0.;
+    cell_reverse(&m, seg + c * m.Q, lam + c * m.Q, li, gamma[c], &dg);
+    sens[c] += dg;
   }
   free(ck); free(seg); free(f); free(tmp); free(lam);
   return 0;

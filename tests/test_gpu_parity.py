@@ -1,0 +1,261 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle on the same
+seeded inputs.
+
+Tolerances (norm-wise, max|gpu - oracle| / max|oracle|):
+* FP64 storage: populations, per-step objective, adjoint and dJ/dgamma within 1e-12.
+* FP32 shifted storage: populations within 2e-6, dJ/dgamma within 1e-4 (the
+  target for the FP32 gradient against the FP64 oracle).
+* FP16 storage with FP32 compute: populations within 2e-3.
+"""
+import numpy as np
+import pytest
+
+import lbmgpu as G
+import workloads as W
+from helpers import rel_inf, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def run_forward(cfg, gamma, n, macros=None):
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.init_equilibrium(macros)
+        J, js = h.forward(n, per_step=True)
+        return h.populations(), js, J, h.macros()
+
+
+def run_gradient(cfg, gamma, n, k):
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.init_equilibrium()
+        return h.gradient(n, k)
+
+
+# -- configuration 1: 128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps --------------------
+
+def test_config1_forward_matches_oracle(orc):
+    cfg, gamma, n = W.workload_config1()
+    f, js, J, mac = run_forward(cfg, gamma, n)
+    fo, jo, Jo = orc.forward(cfg, gamma, n)
+    assert rel_inf(f, fo) < FP64_TOL
+    assert rel_inf(js, jo) < FP64_TOL
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    # macros are the reference's: rho = sum f, u = j (incompressible)
+    m = mac.reshape(-1, 3)
+    fr = fo.reshape(-1, 9)
+    assert rel_inf(m[:, 0], fr.sum(axis=1)) < FP64_TOL
+
+
+def test_config1_gradient_matches_oracle(orc):
+    cfg, gamma, _ = W.workload_config1()
+    n = 400
+    cfg = cfg.replace(obj_weight=1.0 / n)
+    J, s, st = run_gradient(cfg, gamma, n, 16)
+    Jo, so = orc.gradient(cfg, gamma, n)
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    assert rel_inf(s, so) < FP64_TOL
+    assert st.recomputed_steps == G.wang_recompute_count(n, 16)
+
+
+def test_unsteady_inlet_and_dissipation_gradient(orc):
+    cfg = W.channel_2d(64, 32, amp=0.2, period=50.0, objective=G.OBJ_DISSIPATION, nsteps=150)
+    gamma = W.design_2d(64, 32, 99)
+    J, s, _ = run_gradient(cfg, gamma, 150, 7)
+    Jo, so = orc.gradient(cfg, gamma, 150)
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+def test_mrt2d_forward_and_gradient(orc):
+    cfg = W.channel_2d(40, 20, collision=G.MRT, nsteps=120)
+    gamma = W.design_2d(40, 20, 5)
+    f, js, J, _ = run_forward(cfg, gamma, 120)
+    fo, jo, Jo = orc.forward(cfg, gamma, 120)
+    assert rel_inf(f, fo) < FP64_TOL
+    Jg, s, _ = run_gradient(cfg, gamma, 120, 4)
+    Jgo, so = orc.gradient(cfg, gamma, 120)
+    assert abs(Jg - Jgo) <= FP64_TOL * abs(Jgo)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+# -- configuration 3 family: D3Q19 MRT + Brinkman duct --------------------------------
+
+def test_d3q19_mrt_forward_matches_oracle(orc):
+    cfg, gamma, _ = W.workload_config3(nx=32, ny=16, nz=12, nsteps=150)
+    f, js, J, mac = run_forward(cfg, gamma, 150)
+    fo, jo, Jo = orc.forward(cfg, gamma, 150)
+    assert rel_inf(f, fo) < FP64_TOL
+    assert rel_inf(js, jo) < FP64_TOL
+
+
+def test_d3q19_mrt_gradient_matches_oracle(orc):
+    cfg, gamma, _ = W.workload_config3(nx=20, ny=12, nz=10, nsteps=80)
+    J, s, st = run_gradient(cfg, gamma, 80, 6)
+    Jo, so = orc.gradient(cfg, gamma, 80)
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+def test_d3q19_bgk_forward_and_gradient(orc):
+    cfg, gamma, _ = W.workload_config3(nx=18, ny=10, nz=9, nsteps=60)
+    cfg = cfg.replace(collision=G.BGK)
+    f, _, _, _ = run_forward(cfg, gamma, 60)
+    fo, _, _ = orc.forward(cfg, gamma, 60)
+    assert rel_inf(f, fo) < FP64_TOL
+    J, s, _ = run_gradient(cfg, gamma, 60, 5)
+    Jo, so = orc.gradient(cfg, gamma, 60)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+# -- thermal double distribution --------------------------------------------------------
+
+def test_thermal_forward_and_gradient(orc):
+    cfg, gamma, _ = W.workload_config4(nx=48, ny=24, nsteps=100)
+    f, js, J, _ = run_forward(cfg, gamma, 100)
+    fo, jo, Jo = orc.forward(cfg, gamma, 100)
+    assert rel_inf(f, fo) < FP64_TOL
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    Jg, s, _ = run_gradient(cfg, gamma, 100, 5)
+    Jgo, so = orc.gradient(cfg, gamma, 100)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+# -- single reverse steps through the step API ----------------------------------------
+
+def test_adjoint_steps_match_oracle(orc):
+    cfg = W.channel_2d(30, 14, nsteps=40)
+    gamma = W.design_2d(30, 14, 3)
+    # forward trajectory from the oracle
+    f = np.zeros(cfg.ncells * 9)
+    import ctypes
+    states = []
+    ft, _, _ = orc.forward(cfg, gamma, 0)
+    states.append(ft.copy())
+    for t in range(1, 41):
+        ft2 = ft.copy()
+        c = cfg.to_c()
+        orc.lib.orc_forward_from(ctypes.byref(c), gamma.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                 ft2.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), t - 1, 1, None, None)
+        ft = ft2
+        states.append(ft.copy())
+    lam_o = np.zeros(cfg.ncells * 9)
+    sens_o = np.zeros(cfg.ncells)
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.adjoint_reset()
+        for t in range(40, 30, -1):
+            h.set_populations(states[t], t)
+            h.adjoint_step()
+            lam_o, sens_o = orc.adjoint_step(cfg, gamma, states[t], t, lam_o, sens_o)
+            assert rel_inf(h.adjoint(), lam_o) < FP64_TOL
+            assert rel_inf(h.sensitivity(), sens_o) < FP64_TOL
+        del f
+
+
+# -- reduced precision against the FP64 oracle -------------------------------------------
+
+def test_fp32_fp16_storage_error_vs_fp64_oracle(orc):
+    cfg, gamma, _ = W.workload_config3(nx=32, ny=16, nz=16, nsteps=200)
+    fo, jo, Jo = orc.forward(cfg, gamma, 200)
+    f32, _, J32, _ = run_forward(cfg.replace(storage=G.STORE_FP32), gamma, 200)
+    f16, _, J16, _ = run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 200)
+    e32, e16 = rel_inf(f32, fo), rel_inf(f16, fo)
+    print("D3Q19 populations after 200 steps: FP32 rel %.3e, FP16 rel %.3e" % (e32, e16))
+    assert e32 < 2e-6
+    assert e16 < 2e-3
+
+
+def test_fp32_gradient_vs_fp64_oracle(orc):
+    cfg, gamma, _ = W.workload_config3(nx=24, ny=12, nz=12, nsteps=120)
+    Jo, so = orc.gradient(cfg, gamma, 120)
+    J, s, _ = run_gradient(cfg.replace(storage=G.STORE_FP32), gamma, 120, 8)
+    e = rel_l2(s, so)
+    print("D3Q19 FP32 gradient rel L2 error %.3e, J rel %.3e" % (e, abs(J - Jo) / abs(Jo)))
+    assert e < 1e-4
+    assert abs(J - Jo) < 1e-4 * abs(Jo)
+
+
+# -- finite differences --------------------------------------------------------------------
+
+def test_gradient_matches_central_differences():
+    """dJ/dgamma against central FD (h = 1e-6, FP64) at seeded cells, the
+    reference's verification (topOpt/finiteDifferenceCheck2d.cc:58-113) with
+    central instead of one-sided differences."""
+    cfg = W.channel_2d(32, 16, amp=0.2, period=30.0, objective=G.OBJ_DISSIPATION, nsteps=80)
+    gamma = W.design_2d(32, 16, 21)
+    _, s, _ = run_gradient(cfg, gamma, 80, 5)
+    rng = np.random.default_rng(12)
+    cells = rng.choice(cfg.ncells, size=8, replace=False)
+    hstep = 1e-6
+    with G.Handle(cfg) as h:
+        for c in cells:
+            vals = []
+            for sgn in (1.0, -1.0):
+                g = gamma.copy()
+                g[c] = min(max(g[c] + sgn * hstep, 0.0), 1.0)
+                h.set_design(g)
+                h.init_equilibrium()
+                vals.append((h.forward(80), g[c]))
+            fd = (vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1])
+            assert abs(fd - s[c]) <= 1e-5 * max(abs(s).max(), 1e-30), (c, fd, s[c])
+
+
+# -- edge cases ------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("nx,ny", [(37, 19), (5, 3), (300, 7)])
+def test_ragged_sizes(orc, nx, ny):
+    cfg = W.channel_2d(nx, ny, nsteps=30)
+    gamma = W.design_2d(nx, ny, nx * 100 + ny)
+    f, js, J, _ = run_forward(cfg, gamma, 30)
+    fo, jo, Jo = orc.forward(cfg, gamma, 30)
+    assert rel_inf(f, fo) < FP64_TOL
+    Jg, s, _ = run_gradient(cfg, gamma, 30, 2)
+    Jgo, so = orc.gradient(cfg, gamma, 30)
+    assert rel_inf(s, so) < FP64_TOL
+
+
+def test_gradient_snapshot_counts_agree():
+    cfg = W.channel_2d(24, 12, nsteps=50)
+    gamma = W.design_2d(24, 12, 8)
+    ref = None
+    for k in (2, 3, 7, 51, 60):
+        J, s, st = run_gradient(cfg, gamma, 50, k)
+        assert st.recomputed_steps == G.wang_recompute_count(50, k)
+        if ref is None:
+            ref = (J, s)
+        else:
+            assert J == ref[0]
+            assert np.array_equal(s, ref[1])   # recomputation is bitwise reproducible
+
+
+def test_single_step_and_roundtrip(orc):
+    cfg = W.channel_2d(20, 10, nsteps=1)
+    gamma = W.design_2d(20, 10, 4)
+    f, js, J, _ = run_forward(cfg, gamma, 1)
+    fo, jo, Jo = orc.forward(cfg, gamma, 1)
+    assert rel_inf(f, fo) < FP64_TOL
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.set_populations(fo, 1)
+        assert h.time() == 1
+        assert np.array_equal(h.populations(), fo)
+
+
+def test_errors_are_reported():
+    cfg = W.channel_2d(20, 10)
+    with G.Handle(cfg) as h:
+        with pytest.raises(G.LBMError) as e:
+            h.forward(3)
+        assert e.value.code == -5
+        g = W.design_2d(20, 10, 1)
+        g[5] = np.nan
+        with pytest.raises(G.LBMError) as e:
+            h.set_design(g)
+        assert e.value.code == -6
+    bad = cfg.replace(omega=2.5)
+    with pytest.raises(G.LBMError) as e:
+        G.Handle(bad)
+    assert e.value.code == -1
