@@ -213,10 +213,16 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnapshots, double* J,
                  double* dJdgamma, lbm_gradient_stats* stats);
 
 /* Device-time measurement for benchmarks: run `nsteps` forward steps
- * (which = 0) or reverse steps over the current state (which = 1; the
- * forward state is left unchanged) on the handle's stream, bracketed by
- * CUDA events recorded on that stream.  *ms gets the elapsed time. */
+ * (which = 0), reverse steps over the current state (which = 1; the forward
+ * state is left unchanged) or forward+reverse pairs (which = 2) on the
+ * handle's stream, bracketed by CUDA events recorded on that stream.  *ms
+ * gets the elapsed time.  The adjoint and sensitivity fields are scratch
+ * afterwards. */
 int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms);
+
+/* Select the CUDA device (ordinal) that handles created afterwards by this
+ * thread use (one process per GPU: the rank's local GPU). */
+int lbm_select_device(int ordinal);
 
 /* Number of kernel launches issued by this handle since creation. */
 int lbm_get_launch_count(const lbm_handle* h, int64_t* launches);

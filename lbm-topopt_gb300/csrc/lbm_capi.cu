@@ -703,10 +703,10 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
 
 int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
-  if (!ms || nsteps < 1 || (which != 0 && which != 1)) return fail(h, LBM_ERR_ARG, "bad arguments");
+  if (!ms || nsteps < 1 || which < 0 || which > 2) return fail(h, LBM_ERR_ARG, "bad arguments");
   if (!h->have_design || !h->have_state) return fail(h, LBM_ERR_STATE, "no design or state");
   int rc;
-  if (which == 1 && !h->have_adjoint) {
+  if (which >= 1 && !h->have_adjoint) {
     if ((rc = zero_adjoint(h))) return rc;
     h->have_adjoint = true;
   }
@@ -714,13 +714,30 @@ int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms) {
   if (which == 1 && h->t < 1) h->t = 1;
   cudaEventRecord(h->ev[0], h->stream);
   for (int k = 0; k < nsteps; ++k) {
-    rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
+    if (which == 0) {
+      rc = forward_step(h, nullptr);
+    } else if (which == 1) {
+      rc = adjoint_step(h);
+    } else {
+      rc = forward_step(h, nullptr);
+      if (!rc) rc = adjoint_step(h);
+    }
     if (rc) return rc;
   }
   cudaEventRecord(h->ev[1], h->stream);
   if ((rc = sync(h))) return rc;
   if (which == 1) h->t = t_keep;
   cudaEventElapsedTime(ms, h->ev[0], h->ev[1]);
+  return LBM_OK;
+}
+
+int lbm_select_device(int ordinal) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return fail(nullptr, LBM_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  if (ordinal < 0 || ordinal >= n) return fail(nullptr, LBM_ERR_ARG, "device %d of %d", ordinal, n);
+  e = cudaSetDevice(ordinal);
+  if (e != cudaSuccess) return fail(nullptr, LBM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
   return LBM_OK;
 }
 

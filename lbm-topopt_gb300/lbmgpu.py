@@ -193,6 +193,7 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_gradient": (C.c_int, [H, C.c_int, C.c_int, dp, dp, C.POINTER(CGradStats)]),
         "lbm_time_steps": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
         "lbm_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
+        "lbm_select_device": (C.c_int, [C.c_int]),
         "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
@@ -208,6 +209,14 @@ def _ptr(a: Optional[np.ndarray]):
     if a is None:
         return None
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def select_device(ordinal: int) -> None:
+    """Use GPU `ordinal` for handles created afterwards by this thread."""
+    lib = load_library()
+    rc = lib.lbm_select_device(int(ordinal))
+    if rc:
+        raise LBMError(rc, lib.lbm_last_error(None).decode())
 
 
 def wang_recompute_count(nsteps: int, nsnapshots: int) -> int:

@@ -21,6 +21,10 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* ------------------------------------------------------------------ */
 /* Lattices: latticeBoltzmann/lattices2d.hh:16-62, lattices3d.hh:141-160 */
@@ -102,7 +106,29 @@ static double backmap_coeff(const double* row, int Q, int i) {
 
 static double MRT2D_B[9][6];
 static double MRT3D_B[19][15];
+
+/* Sparse forms of the tables, same order as the dense loops: the nonzero
+ * entries of each moment row (over i) and of each back-map row (over k). */
+typedef struct {
+  int n;
+  int idx[19];
+  double c[19];
+} sparse_row;
+static sparse_row MRT2D_MS[6], MRT3D_MS[15];   /* rows of M over i */
+static sparse_row MRT2D_BS[9], MRT3D_BS[19];   /* rows of B over k */
+static sparse_row MRT2D_MT[9], MRT3D_MT[19];   /* columns of M (over k) */
 static int mrt_tables_ready = 0;
+
+static void sparse_build(sparse_row* r, const double* v, int n, int stride) {
+  r->n = 0;
+  for (int j = 0; j < n; ++j) {
+    double c = v[j * stride];
+    if (c == 0.) continue;
+    r->idx[r->n] = j;
+    r->c[r->n] = c;
+    r->n++;
+  }
+}
 
 static void mrt_tables_init(void) {
   if (mrt_tables_ready) return;
@@ -110,25 +136,28 @@ static void mrt_tables_init(void) {
     for (int k = 0; k < 6; ++k) MRT2D_B[i][k] = backmap_coeff(MRT2D_M[k], 9, i);
   for (int i = 0; i < 19; ++i)
     for (int k = 0; k < 15; ++k) MRT3D_B[i][k] = backmap_coeff(MRT3D_M[k], 19, i);
+  for (int k = 0; k < 6; ++k) sparse_build(&MRT2D_MS[k], MRT2D_M[k], 9, 1);
+  for (int k = 0; k < 15; ++k) sparse_build(&MRT3D_MS[k], MRT3D_M[k], 19, 1);
+  for (int i = 0; i < 9; ++i) sparse_build(&MRT2D_BS[i], MRT2D_B[i], 6, 1);
+  for (int i = 0; i < 19; ++i) sparse_build(&MRT3D_BS[i], MRT3D_B[i], 15, 1);
+  for (int i = 0; i < 9; ++i) sparse_build(&MRT2D_MT[i], &MRT2D_M[0][i], 6, 9);
+  for (int i = 0; i < 19; ++i) sparse_build(&MRT3D_MT[i], &MRT3D_M[0][i], 15, 19);
   mrt_tables_ready = 1;
 }
 
-/* m_k = sum_i M[k][i] f_i, left to right over i, skipping zero entries. */
-static double row_dot(const double* row, const double* f, int Q) {
-  double s = 0.;
-  int first = 1;
-  for (int i = 0; i < Q; ++i) {
-    double c = row[i];
-    if (c == 0.) continue;
-    double t = (c == 1.) ? f[i] : (c == -1.) ? -f[i] : c * f[i];
-    if (first) {
-      s = t;
-      first = 0;
-    } else if (c == -1.) {
-      s = s - f[i];
-    } else {
-      s = s + t;
-    }
+/* m_k = sum_i M[k][i] f_i, left to right over the nonzero entries. */
+static double row_dot_sparse(const sparse_row* r, const double* f) {
+  const int* ix = r->idx;
+  const double* c = r->c;
+  double s = (c[0] == 1.) ? f[ix[0]] : (c[0] == -1.) ? -f[ix[0]] : c[0] * f[ix[0]];
+  for (int j = 1; j < r->n; ++j) {
+    double cj = c[j], v = f[ix[j]];
+    if (cj == -1.)
+      s = s - v;
+    else if (cj == 1.)
+      s = s + v;
+    else
+      s = s + cj * v;
   }
   return s;
 }
@@ -319,19 +348,31 @@ static void mrt_collide(const model_t* m, const double* fin, double* fout, doubl
   double mo[15];
   int Q = m->Qf, K = (m->dim == 2) ? 6 : 15;
   flow_macros(m, fin, mac);
-  for (int k = 0; k < K; ++k)
-    mo[k] = row_dot(m->dim == 2 ? MRT2D_M[k] : MRT3D_M[k], fin, Q);
-  if (m->dim == 2)
-    mrt2d_relax(mo, mac, m);
-  else
-    mrt3d_relax(mo, mac, m);
-  for (int i = 0; i < Q; ++i) {
-    const double* b = (m->dim == 2) ? MRT2D_B[i] : MRT3D_B[i];
-    double v = fin[i];
-    for (int k = 0; k < K; ++k) {
-      if (b[k] == 0.) continue;
-      v = v + b[k] * mo[k];
+  /* Dense left-to-right sums: the zero entries add exact zeros and products
+   * with +-1 are exact, so the partial sums are those of the reference's
+   * written-out expressions (MRT3d.hh:50-90, 111-175). */
+  if (m->dim == 3) {
+    for (int k = 0; k < 15; ++k) {
+      double acc = 0.;
+      for (int i = 0; i < 19; ++i) acc += MRT3D_M[k][i] * fin[i];
+      mo[k] = acc;
     }
+    mrt3d_relax(mo, mac, m);
+    for (int i = 0; i < 19; ++i) {
+      double v = fin[i];
+      for (int k = 0; k < 15; ++k) v += MRT3D_B[i][k] * mo[k];
+      fout[i] = v;
+    }
+    return;
+  }
+  const sparse_row* MS = MRT2D_MS;
+  const sparse_row* BS = MRT2D_BS;
+  for (int k = 0; k < K; ++k) mo[k] = row_dot_sparse(&MS[k], fin);
+  mrt2d_relax(mo, mac, m);
+  for (int i = 0; i < Q; ++i) {
+    const sparse_row* b = &BS[i];
+    double v = fin[i];
+    for (int j = 0; j < b->n; ++j) v = v + b->c[j] * mo[b->idx[j]];
     fout[i] = v;
   }
 }
@@ -489,21 +530,36 @@ static void rev_mrt(const model_t* m, const double* fin, const double* lo, doubl
                      r[4], r[4], r[4]};
     for (int k = 0; k < 15; ++k) rate[k] = rr[k];
   }
-  for (int k = 0; k < K; ++k) {
-    double s = 0.;
-    for (int i = 0; i < Q; ++i) {
-      const double* b = (m->dim == 2) ? MRT2D_B[i] : MRT3D_B[i];
-      if (b[k] != 0.) s += b[k] * lo[i];
+  if (m->dim == 3) {
+    for (int k = 0; k < 15; ++k) {
+      double acc = 0.;
+      for (int i = 0; i < 19; ++i) acc += MRT3D_B[i][k] * lo[i];
+      a[k] = rate[k] * acc;
     }
-    a[k] = rate[k] * s; /* adjoint of (m_k - meq_k) */
+    for (int i = 0; i < 19; ++i) {
+      double v = lo[i];
+      for (int k = 0; k < 15; ++k) v += MRT3D_M[k][i] * a[k];
+      li[i] += v;
+    }
   }
-  /* through m_k = M f */
-  for (int i = 0; i < Q; ++i) {
-    double v = lo[i];
-    for (int k = 0; k < K; ++k) {
-      double c = (m->dim == 2) ? MRT2D_M[k][i] : MRT3D_M[k][i];
-      if (c != 0.) v += c * a[k];
+  const sparse_row* MS = MRT2D_MS;
+  const sparse_row* MT = MRT2D_MT;
+  for (int k = 0; k < K && m->dim == 2; ++k) {
+    /* sum_i B[i][k] lo_i = -(1/|M_k|^2) sum_i M[k][i] lo_i */
+    const sparse_row* r = &MS[k];
+    double s = 0., n2 = 0.;
+    for (int j = 0; j < r->n; ++j) {
+      s += (-r->c[j]) * lo[r->idx[j]];
+      n2 += r->c[j] * r->c[j];
     }
+    a[k] = rate[k] * (s / n2); /* adjoint of (m_k - meq_k) */
+  }
+  (void)Q;
+  /* through m_k = M f */
+  for (int i = 0; i < Q && m->dim == 2; ++i) {
+    const sparse_row* c = &MT[i];
+    double v = lo[i];
+    for (int j = 0; j < c->n; ++j) v += c->c[j] * a[c->idx[j]];
     li[i] += v;
   }
   /* through -meq(rho, j) */
@@ -1097,12 +1153,20 @@ static void collide_all(const model_t* m, double* F, const double* gamma) {
   }
 }
 
+static void copy_par(double* dst, const double* src, int64_t n) {
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < (n + 4095) / 4096; ++b) {
+    int64_t lo = b * 4096, len = (n - lo < 4096) ? n - lo : 4096;
+    memcpy(dst + lo, src + lo, sizeof(double) * len);
+  }
+}
+
 /* f_{t+1} = BC_{t+1}(stream(collide(f_t))) ; F holds f_t on entry, f_{t+1} on exit. */
 static void step(const model_t* m, double* F, double* tmp, const double* gamma, int t) {
   collide_all(m, F, gamma);
   stream_all(m, F, tmp);
   apply_bcs(m, t + 1, tmp);
-  memcpy(F, tmp, sizeof(double) * m->ncell * m->Q);
+  copy_par(F, tmp, m->ncell * m->Q);
 }
 
 /* One reverse step at f_t (t >= 1): lam holds the adjoint of the post-collision
@@ -1123,7 +1187,7 @@ static void adjoint_step(const model_t* m, const double* F, double* lam, double*
   /* AdjointLBSolver::adjointStream (adjointLBSolver.cc:50-81) */
   adjoint_bcs(m, t, lam);
   adjoint_stream_all(m, lam, tmp);
-  memcpy(lam, tmp, sizeof(double) * m->ncell * m->Q);
+  copy_par(lam, tmp, m->ncell * m->Q);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1448,4 +1512,55 @@ int orc_wang_count(int nsteps, int nsnap, int64_t* recomputed, int* ok_out) {
   if (ok_out) *ok_out = ok;
   free(w.n); free(w.freeq); free(w.avail); free(w.slot_state);
   return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* CPU baseline timing: wall time of nsteps forward steps and of nsteps reverse
+ * steps of this restatement on nthreads host threads (0 = all). */
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int orc_time_steps(const lbm_config* cfg, const double* gamma, int nsteps, int nthreads,
+                   double* sec_fwd, double* sec_adj) {
+  model_t m;
+  if (model_init(&m, cfg)) return -1;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  int64_t S = m.ncell * m.Q;
+  double* f = (double*)malloc(sizeof(double) * S);
+  double* tmp = (double*)malloc(sizeof(double) * S);
+  double* lam = (double*)calloc(S, sizeof(double));
+  double* sens = (double*)calloc(m.ncell, sizeof(double));
+  if (!f || !tmp || !lam || !sens) {
+    free(f); free(tmp); free(lam); free(sens);
+    return -4;
+  }
+  init_equilibrium(&m, NULL, f);
+  double t0 = now_s();
+  for (int t = 0; t < nsteps; ++t) {
+    step(&m, f, tmp, gamma, t);
+    (void)objective(&m, f, gamma);
+  }
+  double t1 = now_s();
+  for (int t = nsteps; t >= 1; --t) adjoint_step(&m, f, lam, tmp, gamma, sens, t);
+  double t2 = now_s();
+  if (sec_fwd) *sec_fwd = t1 - t0;
+  if (sec_adj) *sec_adj = t2 - t1;
+  free(f); free(tmp); free(lam); free(sens);
+  return 0;
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_num_procs();
+#else
+  return 1;
+#endif
 }
