@@ -283,6 +283,7 @@ def main():
     h = G.Handle(cfg)
     h.set_design(gamma)
     h.init_equilibrium()
+    shapes = h.autotune()   # thread-block shapes of the two step kernels
     h.forward(20)   # develop the inflow before timing
     # warm-up pairs
     h.time_steps(2, args.warmup)
@@ -365,6 +366,9 @@ def main():
 
     # FP64 storage: same gradient, for the FP32-vs-FP64 comparison
     h64 = G.Handle(cfg.replace(storage=G.STORE_FP64))
+    h64.set_design(gamma)
+    h64.init_equilibrium()
+    h64.autotune(2)
     one_gradient(h64)
     t0 = time.perf_counter()
     one_gradient(h64)
@@ -389,7 +393,8 @@ def main():
         "config": {"workload": CONFIG_NAME, "cells": cells,
                    "step": "one forward + one adjoint time step over the lattice",
                    "l2": "inputs larger than L2 (FP32 state 319 MB > 129 MB L2); no flush",
-                   "parallelism": "replicas (one independent duct per GPU)"},
+                   "parallelism": "replicas (one independent duct per GPU)",
+                   "block_shapes": {"forward": list(shapes[0]), "adjoint": list(shapes[1])}},
         "mlups_fwd": round(cells * args.steps / (ms_fwd * 1e-3) / 1e6, 2),
         "mlups_adj": round(cells * args.steps / (ms_adj * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "kernel": "k_adjoint<D3Q19,MRT,float>",

@@ -220,6 +220,15 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnapshots, double* J,
  * afterwards. */
 int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms);
 
+/* Time every candidate thread-block shape of the forward and reverse step
+ * kernels for nsteps steps each on this handle's lattice and keep the
+ * fastest (the tile-shape autotuner).  Needs a design and a state; the state
+ * is left unchanged and the adjoint and sensitivity fields are zeroed. */
+int lbm_autotune(lbm_handle* h, int nsteps);
+
+/* Block shape in use for the forward (which = 0) or reverse (which = 1) step. */
+int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by);
+
 /* Select the CUDA device (ordinal) that handles created afterwards by this
  * thread use (one process per GPU: the rank's local GPU). */
 int lbm_select_device(int ordinal);

@@ -4,7 +4,9 @@
 // is no host fallback.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -30,6 +32,17 @@ struct Geometry {
   unsigned nblocks;
 };
 
+Geometry make_geometry(int nx, int ny, int nz, int bx, int by) {
+  Geometry g;
+  g.block = dim3(bx, by, 1);
+  g.grid = dim3((nx + bx - 1) / bx, (ny + by - 1) / by, nz);
+  g.nblocks = g.grid.x * g.grid.y * g.grid.z;
+  return g;
+}
+
+// Thread-block shapes the autotuner tries (x-major rows; 128 or 256 threads).
+const int kShapes[][2] = {{256, 1}, {128, 2}, {64, 4}, {32, 8}, {128, 1}, {64, 2}, {32, 4}};
+
 }  // namespace
 
 struct lbm_handle {
@@ -42,7 +55,11 @@ struct lbm_handle {
   size_t gam_bytes = 0;  // bytes per design value
   LaunchFn launch = nullptr;
   cudaStream_t stream = nullptr;
-  Geometry geo;
+  Geometry geo;       // initialisation / export kernels
+  Geometry geo_fwd;   // forward step (autotuned)
+  Geometry geo_adj;   // reverse step (autotuned)
+  bool tuned = false;
+  size_t partial_cap = 0;
   void* f[2] = {nullptr, nullptr};
   int cur = 0;
   void* gamma = nullptr;
@@ -56,6 +73,8 @@ struct lbm_handle {
   double* stage = nullptr;     // FP64 AoS staging (ncell*Q)
   double* init_mac = nullptr;  // initial macros kept for lbm_gradient (device, may be null)
   std::vector<void*> slots;
+  double* bcprof_d[LBM_MAX_BC] = {};   // inflow profile per boundary (device)
+  float* bcprof_f[LBM_MAX_BC] = {};
   int t = 0;
   bool have_design = false, have_state = false, have_adjoint = false;
   int64_t launches = 0;
@@ -175,6 +194,12 @@ void destroy_buffers(lbm_handle* h) {
   void* ps[] = {h->gamma, h->sens, h->partial, h->counter, h->jdev, h->stage, h->init_mac};
   for (void* p : ps)
     if (p) cudaFree(p);
+  for (int k = 0; k < LBM_MAX_BC; ++k) {
+    if (h->bcprof_d[k]) cudaFree(h->bcprof_d[k]);
+    if (h->bcprof_f[k]) cudaFree(h->bcprof_f[k]);
+    h->bcprof_d[k] = nullptr;
+    h->bcprof_f[k] = nullptr;
+  }
   h->gamma = h->sens = h->partial = nullptr;
   h->counter = nullptr;
   h->jdev = h->stage = h->init_mac = nullptr;
@@ -216,6 +241,12 @@ KParams base_params(const lbm_handle* h, int t) {
     // value(t) = value * (1 + amp sin(2 pi t / period)), evaluated here once per launch
     double tf = (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
     d.value = b.value * tf;
+    d.value_f = (float)d.value;
+    d.vshift = d.value - 1.;
+    d.vshift_f = (float)d.vshift;
+    d.prof = h->bcprof_d[k];
+    d.prof_f = h->bcprof_f[k];
+    d.ny_box = b.box[3] - b.box[2] + 1;
   }
   p.objective = c.objective;
   p.obj_weight = c.obj_weight;
@@ -229,6 +260,37 @@ KParams base_params(const lbm_handle* h, int t) {
     p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
     p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
   }
+  ModelParams<double>& md = p.md;
+  md.omega = c.omega;
+  for (int i = 0; i < 8; ++i) md.mrt[i] = c.mrt[i];
+  md.pbb_scale = c.interp_scale;
+  md.pbb_q = c.interp_q;
+  md.diff = c.diffusivity;
+  md.ramp_q = c.ramp_q;
+  md.ramp_ck = c.ramp_ck;
+  md.heat_rate = c.heat_rate;
+  md.heat_T = c.heat_T;
+  md.obj_weight = c.obj_weight;
+  md.w_in = p.inv_in * c.obj_weight;
+  md.w_out = p.inv_out * c.obj_weight;
+  {
+    double nu = (1. / c.omega - 0.5) / 3.;
+    md.cv_diss = 4.5 * nu * c.omega * c.omega;
+  }
+  ModelParams<float>& mf = p.mf;
+  mf.omega = (float)md.omega;
+  for (int i = 0; i < 8; ++i) mf.mrt[i] = (float)md.mrt[i];
+  mf.pbb_scale = (float)md.pbb_scale;
+  mf.pbb_q = (float)md.pbb_q;
+  mf.diff = (float)md.diff;
+  mf.ramp_q = (float)md.ramp_q;
+  mf.ramp_ck = (float)md.ramp_ck;
+  mf.heat_rate = (float)md.heat_rate;
+  mf.heat_T = (float)md.heat_T;
+  mf.obj_weight = (float)md.obj_weight;
+  mf.w_in = (float)md.w_in;
+  mf.w_out = (float)md.w_out;
+  mf.cv_diss = (float)md.cv_diss;
   p.partial = h->partial;
   p.counter = h->counter;
   p.gamma = h->gamma;
@@ -237,7 +299,8 @@ KParams base_params(const lbm_handle* h, int t) {
 }
 
 int launch(lbm_handle* h, int kind, const KParams& p, double* aux) {
-  h->launch(kind, h->geo.grid, h->geo.block, h->stream, p, aux);
+  const Geometry& g = kind == K_FORWARD ? h->geo_fwd : kind == K_ADJOINT ? h->geo_adj : h->geo;
+  h->launch(kind, g.grid, g.block, h->stream, p, aux);
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(h, LBM_ERR_CUDA, "kernel launch %d: %s", kind, cudaGetErrorString(e));
@@ -367,6 +430,11 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   h->nmac = c.lattice == LBM_D2Q9 ? 3 : 4;
   h->ncell = (int64_t)c.nx * c.ny * h->cfg.nz;
   h->P = (h->ncell + 127) / 128 * 128;
+  if ((int64_t)h->Q * h->P >= (int64_t)INT32_MAX) {
+    delete h;
+    return fail(nullptr, LBM_ERR_SUP, "lattice of %lld cells too large for 32-bit population offsets",
+                (long long)h->ncell);
+  }
   h->pop_bytes = c.storage == LBM_STORE_FP64 ? 8 : c.storage == LBM_STORE_FP32 ? 4 : 2;
   h->adj_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
   h->gam_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
@@ -383,9 +451,14 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   if (bx > 256) bx = 256;
   int by = kBlockThreads / bx;
   if (by < 1) by = 1;
-  h->geo.block = dim3(bx, by, 1);
-  h->geo.grid = dim3((c.nx + bx - 1) / bx, (c.ny + by - 1) / by, h->cfg.nz);
-  h->geo.nblocks = h->geo.grid.x * h->geo.grid.y * h->geo.grid.z;
+  h->geo = make_geometry(c.nx, c.ny, h->cfg.nz, bx, by);
+  h->geo_fwd = h->geo;
+  h->geo_adj = h->geo;
+  // partial sums: room for the largest grid any tuned shape can give
+  for (const auto& sh : kShapes) {
+    Geometry g = make_geometry(c.nx, c.ny, h->cfg.nz, sh[0], sh[1]);
+    if (g.nblocks > h->partial_cap) h->partial_cap = g.nblocks;
+  }
 
 #define ALLOC(ptr, bytes)                                                                  \
   do {                                                                                     \
@@ -410,8 +483,34 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   ALLOC(h->lam[1], adjoint_bytes(h));
   ALLOC(h->gamma, (size_t)h->P * h->gam_bytes);
   ALLOC(h->sens, (size_t)h->P * sizeof(double));
-  ALLOC(h->partial, (size_t)h->geo.nblocks * sizeof(double));
+  ALLOC(h->partial, h->partial_cap * sizeof(double));
   ALLOC(h->counter, sizeof(unsigned));
+  // Inflow profile factors over each velocity boundary box, tabulated once:
+  // (m^2 - (y-m)^2)/m^2 with m = (ny-1)/2 (applications/diffuser/diffuser.cc:22-31),
+  // times the same in z on D3Q19.
+  for (int k = 0; k < c.nbc; ++k) {
+    const lbm_bc& b = c.bc[k];
+    if (b.kind != LBM_BC_VELOCITY || b.profile != LBM_PROFILE_PARABOLIC) continue;
+    const int nyb = b.box[3] - b.box[2] + 1, nzb = b.box[5] - b.box[4] + 1;
+    std::vector<double> pd((size_t)nyb * nzb);
+    std::vector<float> pf(pd.size());
+    for (int z = b.box[4]; z <= b.box[5]; ++z)
+      for (int y = b.box[2]; y <= b.box[3]; ++y) {
+        double mid = (double)(c.ny - 1) / 2.;
+        double pr = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
+        if (h->dim == 3) {
+          double mz = (double)(h->cfg.nz - 1) / 2.;
+          pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
+        }
+        size_t i = (size_t)(z - b.box[4]) * nyb + (y - b.box[2]);
+        pd[i] = pr;
+        pf[i] = (float)pr;
+      }
+    ALLOC(h->bcprof_d[k], pd.size() * sizeof(double));
+    ALLOC(h->bcprof_f[k], pf.size() * sizeof(float));
+    cudaMemcpy(h->bcprof_d[k], pd.data(), pd.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(h->bcprof_f[k], pf.data(), pf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
 #undef ALLOC
   cudaMemsetAsync(h->counter, 0, sizeof(unsigned), h->stream);
   cudaMemsetAsync(h->f[0], 0, state_bytes(h), h->stream);
@@ -728,6 +827,62 @@ int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms) {
   if ((rc = sync(h))) return rc;
   if (which == 1) h->t = t_keep;
   cudaEventElapsedTime(ms, h->ev[0], h->ev[1]);
+  return LBM_OK;
+}
+
+int lbm_autotune(lbm_handle* h, int nsteps) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!h->have_design || !h->have_state) return fail(h, LBM_ERR_STATE, "no design or state");
+  if (nsteps < 1) nsteps = 5;
+  int rc;
+  // keep the state: the trial steps run on a copy
+  void* keep = nullptr;
+  CUDA_OR_FAIL(h, cudaMalloc(&keep, state_bytes(h)));
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(keep, h->f[h->cur], state_bytes(h), cudaMemcpyDeviceToDevice, h->stream));
+  const int t_keep = h->t, cur_keep = h->cur;
+  if (!h->have_adjoint) {
+    if ((rc = zero_adjoint(h))) { cudaFree(keep); return rc; }
+    h->have_adjoint = true;
+  }
+  if (h->t < 1) h->t = 1;
+  float best_f = 1e30f, best_a = 1e30f;
+  Geometry bf = h->geo_fwd, ba = h->geo_adj;
+  const int nx = h->cfg.nx;
+  for (const auto& sh : kShapes) {
+    if (sh[0] > ((nx + 31) / 32) * 32 && sh[0] > 32) continue;
+    Geometry g = make_geometry(nx, h->cfg.ny, h->cfg.nz, sh[0], sh[1]);
+    for (int which = 0; which < 2; ++which) {
+      (which == 0 ? h->geo_fwd : h->geo_adj) = g;
+      // one untimed launch, then nsteps timed
+      rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
+      if (rc) { cudaFree(keep); return rc; }
+      cudaEventRecord(h->ev[0], h->stream);
+      for (int k = 0; k < nsteps && !rc; ++k) rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
+      cudaEventRecord(h->ev[1], h->stream);
+      if (rc || (rc = sync(h))) { cudaFree(keep); return rc; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+      if (which == 0 && ms < best_f) { best_f = ms; bf = g; }
+      if (which == 1 && ms < best_a) { best_a = ms; ba = g; }
+    }
+  }
+  h->geo_fwd = bf;
+  h->geo_adj = ba;
+  h->tuned = true;
+  h->cur = cur_keep;
+  h->t = t_keep;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(h->f[h->cur], keep, state_bytes(h), cudaMemcpyDeviceToDevice, h->stream));
+  rc = zero_adjoint(h);
+  if (!rc) rc = sync(h);
+  cudaFree(keep);
+  return rc;
+}
+
+int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by) {
+  if (!h || !bx || !by || which < 0 || which > 1) return fail(nullptr, LBM_ERR_ARG, "bad arguments");
+  const Geometry& g = which == 0 ? h->geo_fwd : h->geo_adj;
+  *bx = g.block.x;
+  *by = g.block.y;
   return LBM_OK;
 }
 

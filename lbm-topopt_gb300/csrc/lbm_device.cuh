@@ -14,11 +14,25 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/lbmgpu.h"
 
 namespace lbm {
 
 enum { LAT_D2Q9 = 0, LAT_D3Q19 = 1, LAT_D2Q9_D2Q5 = 2 };
+
+// Compile-time loop: calls f(std::integral_constant<int, I>) for I = 0..N-1,
+// so that lattice tables and moment coefficients are constant expressions in
+// the body (folded into immediates; register arrays indexed statically).
+template <class F, int... Is>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
 
 // ---------------------------------------------------------------------------
 // Lattices (latticeBoltzmann/lattices2d.hh:16-62, lattices3d.hh:141-160).  The
@@ -146,7 +160,49 @@ struct GammaT<double> {
 struct DevBC {
   int kind, face, profile;
   int box[6];
-  double value;   // value * (1 + amp sin(2 pi t / period)) at this launch's time t
+  double value;       // value * (1 + amp sin(2 pi t / period)) at this launch's time t
+  float value_f;      // the same in FP32
+  double vshift;      // value - 1 (pressure on shifted populations)
+  float vshift_f;
+  const double* prof;   // inflow profile factor over the box, (z-z0)*ny_box + (y-y0); null = 1
+  const float* prof_f;
+  int ny_box;
+};
+
+template <class C>
+__device__ __forceinline__ C bc_value(const DevBC& b);
+template <>
+__device__ __forceinline__ double bc_value<double>(const DevBC& b) { return b.value; }
+template <>
+__device__ __forceinline__ float bc_value<float>(const DevBC& b) { return b.value_f; }
+template <class C>
+__device__ __forceinline__ C bc_vshift(const DevBC& b);
+template <>
+__device__ __forceinline__ double bc_vshift<double>(const DevBC& b) { return b.vshift; }
+template <>
+__device__ __forceinline__ float bc_vshift<float>(const DevBC& b) { return b.vshift_f; }
+template <class C>
+__device__ __forceinline__ C bc_prof(const DevBC& b, int y, int z);
+template <>
+__device__ __forceinline__ double bc_prof<double>(const DevBC& b, int y, int z) {
+  return b.prof ? b.prof[(z - b.box[4]) * b.ny_box + (y - b.box[2])] : 1.;
+}
+template <>
+__device__ __forceinline__ float bc_prof<float>(const DevBC& b, int y, int z) {
+  return b.prof_f ? b.prof_f[(z - b.box[4]) * b.ny_box + (y - b.box[2])] : 1.f;
+}
+
+// Model constants in one precision.  KParams carries an FP64 and an FP32 copy
+// so that FP32 kernels never convert FP64 launch parameters per thread (GB300
+// runs FP64 on a narrow pipe).
+template <class C>
+struct ModelParams {
+  C omega;
+  C mrt[8];
+  C pbb_scale, pbb_q;
+  C diff, ramp_q, ramp_ck, heat_rate, heat_T;
+  C obj_weight, w_in, w_out;   // w_in = inv_in*obj_weight, w_out = inv_out*obj_weight
+  C cv_diss;                   // (9/2) nu omega^2 of the dissipation objective
 };
 
 struct KParams {
@@ -157,6 +213,8 @@ struct KParams {
   double mrt[8];
   double pbb_scale, pbb_q;
   double diff, ramp_q, ramp_ck, heat_rate, heat_T;
+  ModelParams<double> md;
+  ModelParams<float> mf;
   // boundary conditions of the input state's time step
   int nbc;
   int apply_bc;
@@ -178,6 +236,17 @@ struct KParams {
   double* sens;
   int* error_flag;         // set to a non-zero code on a non-finite result
 };
+
+template <class C>
+__device__ __forceinline__ const ModelParams<C>& mp(const KParams& p);
+template <>
+__device__ __forceinline__ const ModelParams<double>& mp<double>(const KParams& p) {
+  return p.md;
+}
+template <>
+__device__ __forceinline__ const ModelParams<float>& mp<float>(const KParams& p) {
+  return p.mf;
+}
 
 __host__ __device__ inline bool in_box(const int* b, int x, int y, int z) {
   return x >= b[0] && x <= b[1] && y >= b[2] && y <= b[3] && z >= b[4] && z <= b[5];
@@ -230,16 +299,16 @@ __device__ __forceinline__ void flow_macros(const C* f, C& rho, C& jx, C& jy, C&
     jx = C(0.);
     jy = C(0.);
     jz = C(0.);
-#pragma unroll
-    for (int i = 0; i < L::QF; ++i) {
+    static_for<L::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
       rho += f[i];
-      if (L::ex(i) == 1) jx += f[i];
-      if (L::ex(i) == -1) jx -= f[i];
-      if (L::ey(i) == 1) jy += f[i];
-      if (L::ey(i) == -1) jy -= f[i];
-      if (L::ez(i) == 1) jz += f[i];
-      if (L::ez(i) == -1) jz -= f[i];
-    }
+      if constexpr (L::ex(i) == 1) jx += f[i];
+      if constexpr (L::ex(i) == -1) jx -= f[i];
+      if constexpr (L::ey(i) == 1) jy += f[i];
+      if constexpr (L::ey(i) == -1) jy -= f[i];
+      if constexpr (L::ez(i) == 1) jz += f[i];
+      if constexpr (L::ez(i) == -1) jz -= f[i];
+    });
   }
 }
 
@@ -292,29 +361,32 @@ struct MRT {
   __host__ __device__ static constexpr int n(int k) { return DIM == 2 ? mrt2d_n(k) : mrt3d_n(k); }
 };
 
-// sum_i M[k][i] f_i, left to right, skipping zeros (folds to adds with the
-// constant row).
-template <int DIM, class C>
-__device__ __forceinline__ C mrt_moment(int k, const C* f) {
+// sum_i M[k][i] f_i, left to right over the nonzero entries of the constant
+// row (0 + first term is exact, so this is the reference's expression).
+template <int DIM, int K, class C>
+__device__ __forceinline__ C mrt_moment(const C* f) {
   using M = MRT<DIM>;
   C s = C(0.);
-  bool first = true;
-#pragma unroll
-  for (int i = 0; i < M::QF; ++i) {
-    const int c = M::m(k, i);
-    if (c == 0) continue;
-    if (first) {
-      s = (c == 1) ? f[i] : (c == -1) ? -f[i] : C(c) * f[i];
-      first = false;
-    } else if (c == 1) {
+  static_for<M::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int c = M::m(K, i);
+    if constexpr (c == 1) {
       s = s + f[i];
-    } else if (c == -1) {
+    } else if constexpr (c == -1) {
       s = s - f[i];
-    } else {
+    } else if constexpr (c != 0) {
       s = s + C(c) * f[i];
     }
-  }
+  });
   return s;
+}
+
+template <int DIM, class C>
+__device__ __forceinline__ void mrt_moments(const C* f, C* mo) {
+  static_for<MRT<DIM>::K>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    mo[k] = mrt_moment<DIM, k>(f);
+  });
 }
 
 // Relaxation r_k = s_k (m_k - meq_k) written as the reference does
@@ -322,7 +394,7 @@ __device__ __forceinline__ C mrt_moment(int k, const C* f) {
 // value (rho, or rho - 1 for shifted storage).
 template <class C>
 __device__ __forceinline__ void mrt2d_relax(C* mo, C rho, C jx, C jy, const KParams& p) {
-  const C s1 = C(p.mrt[0]), s2 = C(p.mrt[1]), s46 = C(p.mrt[2]), om = C(p.omega);
+  const C s1 = mp<C>(p).mrt[0], s2 = mp<C>(p).mrt[1], s46 = mp<C>(p).mrt[2], om = mp<C>(p).omega;
   C uSqr = jx * jx + jy * jy;
   mo[0] = s1 * (mo[0] + C(2.) * rho - C(3.) * uSqr);
   mo[1] = s2 * (mo[1] - rho + C(3.) * uSqr);
@@ -334,9 +406,9 @@ __device__ __forceinline__ void mrt2d_relax(C* mo, C rho, C jx, C jy, const KPar
 
 template <class C>
 __device__ __forceinline__ void mrt3d_relax(C* mo, C rho, C jx, C jy, C jz, const KParams& p) {
-  const C s1 = C(p.mrt[0]), s2 = C(p.mrt[1]), s4 = C(p.mrt[2]), s10 = C(p.mrt[3]),
-          s16 = C(p.mrt[4]), we = C(p.mrt[5]), wej = C(p.mrt[6]), wxx = C(p.mrt[7]),
-          om = C(p.omega);
+  const C s1 = mp<C>(p).mrt[0], s2 = mp<C>(p).mrt[1], s4 = mp<C>(p).mrt[2], s10 = mp<C>(p).mrt[3],
+          s16 = mp<C>(p).mrt[4], we = mp<C>(p).mrt[5], wej = mp<C>(p).mrt[6], wxx = mp<C>(p).mrt[7],
+          om = mp<C>(p).omega;
   C jSqr = jx * jx + jy * jy + jz * jz;
   mo[0] = s1 * (mo[0] + C(11.) * rho - C(19.) * jSqr);
   mo[1] = s2 * (mo[1] - we * rho - wej * jSqr);
@@ -357,21 +429,242 @@ __device__ __forceinline__ void mrt3d_relax(C* mo, C rho, C jx, C jy, C jz, cons
   mo[14] *= s16;
 }
 
-// f_out_i = f_i - sum_k (M[k][i]/N_k) r_k, in k order.
+// f_out_i = f_i - sum_k (M[k][i]/N_k) r_k, in k order, coefficients folded at
+// compile time.
 template <int DIM, class C>
 __device__ __forceinline__ void mrt_backmap(C* f, const C* mo) {
   using M = MRT<DIM>;
-#pragma unroll
-  for (int i = 0; i < M::QF; ++i) {
+  static_for<M::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
     C v = f[i];
-#pragma unroll
-    for (int k = 0; k < M::K; ++k) {
-      const int c = M::m(k, i);
-      if (c == 0) continue;
-      v = v + C(-(double)c / (double)M::n(k)) * mo[k];
-    }
+    static_for<M::K>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      constexpr int c = M::m(k, i);
+      if constexpr (c != 0) {
+        constexpr double b = -(double)c / (double)M::n(k);
+        v = v + C(b) * mo[k];
+      }
+    });
     f[i] = v;
-  }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// D3Q19 MRT + partial bounce-back in population-pair form.  With
+// s_d = f_d + f_{d+9} and a_d = f_d - f_{d+9} (d = 1..9, opp(d) = d+9), the
+// even moments (e, eps, p, pi; MRT3d.hh:50-90 rows 0,1,5-11) are sums over f_0
+// and s_d, the odd ones (q, m; rows 2-4, 12-14) sums over a_d, and the
+// back-map f_i - sum_k (M[k][i]/N_k) r_k splits the same way.  Partial
+// bounce-back (partialBouncebackCollision.hh:53-65) leaves s_d unchanged and
+// scales a_d by (1 - 2 imult).  Same operator as the reference, about half the
+// arithmetic.
+
+// Row k is even (f_d and f_opp(d) weighted alike) or odd (opposite weights);
+// every row of the D3Q19 basis is one or the other.
+__host__ __device__ constexpr bool mrt3d_even(int k) {
+  for (int d = 1; d <= 9; ++d)
+    if (mrt3d_m(k, d) != mrt3d_m(k, d + 9)) return false;
+  return true;
+}
+__host__ __device__ constexpr bool mrt3d_odd(int k) {
+  if (mrt3d_m(k, 0) != 0) return false;
+  for (int d = 1; d <= 9; ++d)
+    if (mrt3d_m(k, d) != -mrt3d_m(k, d + 9)) return false;
+  return true;
+}
+static_assert(mrt3d_even(0) && mrt3d_even(1) && mrt3d_odd(2) && mrt3d_odd(3) && mrt3d_odd(4) &&
+                  mrt3d_even(5) && mrt3d_even(11) && mrt3d_odd(12) && mrt3d_odd(14),
+              "D3Q19 moment rows must split into even and odd rows");
+
+// d(meq_k)/d(rho) and d(meq_k)/d(j_a) of MRT3d.hh:92-109 are applied inline below.
+
+template <class C>
+__device__ __forceinline__ void mrt3d_pair_moments(const C* f, C* s, C* a, C& rho, C& jx, C& jy,
+                                                   C& jz, C* mo) {
+  using L = Lattice<LAT_D3Q19>;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    s[d] = f[d] + f[d + 9];
+    a[d] = f[d] - f[d + 9];
+  });
+  rho = f[0];
+  jx = C(0.);
+  jy = C(0.);
+  jz = C(0.);
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    rho += s[d];
+    if constexpr (L::ex(d) == 1) jx += a[d];
+    if constexpr (L::ex(d) == -1) jx -= a[d];
+    if constexpr (L::ey(d) == 1) jy += a[d];
+    if constexpr (L::ey(d) == -1) jy -= a[d];
+    if constexpr (L::ez(d) == 1) jz += a[d];
+    if constexpr (L::ez(d) == -1) jz -= a[d];
+  });
+  static_for<15>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    C acc = C(0.);
+    if constexpr (mrt3d_even(k)) {
+      constexpr int c0 = mrt3d_m(k, 0);
+      if constexpr (c0 != 0) acc = C(c0) * f[0];
+    }
+    static_for<9>([&](auto D) {
+      constexpr int d = decltype(D)::value + 1;
+      constexpr int c = mrt3d_m(k, d);
+      const C v = mrt3d_even(k) ? s[d] : a[d];
+      if constexpr (c == 1) {
+        acc += v;
+      } else if constexpr (c == -1) {
+        acc -= v;
+      } else if constexpr (c != 0) {
+        acc += C(c) * v;
+      }
+    });
+    mo[k] = acc;
+  });
+}
+
+// In place: f <- PBB(MRT(f)); returns the macros of the input.
+template <class C>
+__device__ __forceinline__ void mrt3d_pair_collide(C* f, C imult, C& rho, C& jx, C& jy, C& jz,
+                                                   const KParams& p) {
+  C s[10], a[10], mo[15];
+  mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, mo);
+  mrt3d_relax(mo, rho, jx, jy, jz, p);
+  // rest population: f_0 - sum_even (M[k][0]/N_k) r_k
+  C f0 = f[0];
+  static_for<15>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    constexpr int c = mrt3d_m(k, 0);
+    if constexpr (mrt3d_even(k) && c != 0) {
+      constexpr double b = -(double)c / (double)mrt3d_n(k);
+      f0 += C(b) * mo[k];
+    }
+  });
+  f[0] = f0;
+  const C keep = C(1.) - C(2.) * imult;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    C E = C(0.), O = C(0.);
+    static_for<15>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      constexpr int c = mrt3d_m(k, d);
+      if constexpr (c != 0) {
+        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
+        if constexpr (mrt3d_even(k))
+          E += C(b) * mo[k];
+        else
+          O += C(b) * mo[k];
+      }
+    });
+    const C sp = s[d] + E;
+    const C ap = (a[d] + O) * keep;
+    f[d] = C(0.5) * (sp + ap);
+    f[d + 9] = C(0.5) * (sp - ap);
+  });
+}
+
+// Transpose of mrt3d_pair_collide at input fin: lam (adjoint of the output)
+// in, adjoint of the input out; dg += dimult * d(out)/d(imult)^T lam.
+template <class C>
+__device__ __forceinline__ void mrt3d_pair_reverse(const C* fin, C* lam, C imult, C dimult, C& dg,
+                                                   const KParams& p) {
+  C s[10], a[10], mo[15];
+  C rho, jx, jy, jz;
+  mrt3d_pair_moments(fin, s, a, rho, jx, jy, jz, mo);
+  mrt3d_relax(mo, rho, jx, jy, jz, p);
+  // adjoints of s' and a'' from the output pairs; imult adjoint from a' = a + 2 O
+  const C keep = C(1.) - C(2.) * imult;
+  C sb[10], ab[10];
+  C imultRev = C(0.);
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    C O = C(0.);
+    static_for<15>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      constexpr int c = mrt3d_m(k, d);
+      if constexpr (c != 0 && !mrt3d_even(k)) {
+        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
+        O += C(b) * mo[k];
+      }
+    });
+    const C ap = a[d] + O;                      // a' before partial bounce-back
+    sb[d] = C(0.5) * (lam[d] + lam[d + 9]);      // adjoint of s'
+    const C ab2 = C(0.5) * (lam[d] - lam[d + 9]);  // adjoint of a''
+    imultRev -= C(2.) * ap * ab2;
+    ab[d] = keep * ab2;                          // adjoint of a'
+  });
+  dg += dimult * imultRev;
+  const C f0b = lam[0];
+  // adjoint of the relaxed moments, then of (m_k - meq_k)
+  const C* rt = mp<C>(p).mrt;
+  const C om = mp<C>(p).omega;
+  C mb[15];
+  static_for<15>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    C acc = C(0.);
+    if constexpr (mrt3d_even(k)) {
+      constexpr int c0 = mrt3d_m(k, 0);
+      if constexpr (c0 != 0) {
+        constexpr double b0 = -(double)c0 / (double)mrt3d_n(k);
+        acc += C(b0) * f0b;
+      }
+    }
+    static_for<9>([&](auto D) {
+      constexpr int d = decltype(D)::value + 1;
+      constexpr int c = mrt3d_m(k, d);
+      if constexpr (c != 0) {
+        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
+        acc += C(b) * (mrt3d_even(k) ? sb[d] : ab[d]);
+      }
+    });
+    // rate of moment k (MRT3d.hh:93-109)
+    C rate;
+    if constexpr (k == 0) rate = rt[0];
+    else if constexpr (k == 1) rate = rt[1];
+    else if constexpr (k >= 2 && k <= 4) rate = rt[2];
+    else if constexpr (k == 6 || k == 8) rate = rt[3];
+    else if constexpr (k >= 12) rate = rt[4];
+    else rate = om;
+    mb[k] = rate * acc;
+  });
+  // through -meq(rho, j)
+  const C we = rt[5], wej = rt[6], wxx = rt[7];
+  const C c2 = C(-2. / 3.);
+  const C a56 = mb[5] + wxx * mb[6], a78 = mb[7] + wxx * mb[8];
+  const C rR = -(mb[0] * C(-11.) + mb[1] * we);
+  const C jR0 = -(mb[0] * C(38.) * jx + mb[1] * C(2.) * wej * jx + mb[2] * c2 + a56 * C(4.) * jx +
+                  mb[9] * jy + mb[11] * jz);
+  const C jR1 = -(mb[0] * C(38.) * jy + mb[1] * C(2.) * wej * jy + mb[3] * c2 - a56 * C(2.) * jy +
+                  a78 * C(2.) * jy + mb[9] * jx + mb[10] * jz);
+  const C jR2 = -(mb[0] * C(38.) * jz + mb[1] * C(2.) * wej * jz + mb[4] * c2 - a56 * C(2.) * jz -
+                  a78 * C(2.) * jz + mb[10] * jy + mb[11] * jx);
+  // through m = M(f0, s, a), rho = f0 + sum s, j = sum e a, and the pair split
+  C f0bar = f0b + rR;
+  static_for<15>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    constexpr int c0 = mrt3d_m(k, 0);
+    if constexpr (mrt3d_even(k) && c0 != 0) f0bar += C(c0) * mb[k];
+  });
+  lam[0] = f0bar;
+  using L = Lattice<LAT_D3Q19>;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    C sbar = sb[d] + rR;
+    C abar = ab[d] + (jR0 * C(L::ex(d)) + jR1 * C(L::ey(d)) + jR2 * C(L::ez(d)));
+    static_for<15>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      constexpr int c = mrt3d_m(k, d);
+      if constexpr (c != 0) {
+        if constexpr (mrt3d_even(k))
+          sbar += C(c) * mb[k];
+        else
+          abar += C(c) * mb[k];
+      }
+    });
+    lam[d] = sbar + abar;
+    lam[d + 9] = sbar - abar;
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -384,8 +677,12 @@ template <int LAT, int COLL, class C>
 __device__ __forceinline__ void flow_collide(C* f, C imult, C& rho, C& jx, C& jy, C& jz,
                                              const KParams& p) {
   using L = Lattice<LAT>;
+  if constexpr (LAT == LAT_D3Q19 && COLL == LBM_MRT) {
+    mrt3d_pair_collide(f, imult, rho, jx, jy, jz, p);
+    return;
+  }
   flow_macros<LAT>(f, rho, jx, jy, jz);
-  const C om = C(p.omega);
+  const C om = mp<C>(p).omega;
   if (COLL == LBM_BGK) {
     if (L::DIM == 2) {
       const C uSqr = jx * jx + jy * jy;
@@ -403,17 +700,16 @@ __device__ __forceinline__ void flow_collide(C* f, C imult, C& rho, C& jx, C& jy
       f[7] = rel * f[7] + om * diagW * (cFeq + C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
     } else {
       const C uSqr = jx * jx + jy * jy + jz * jz;
-#pragma unroll
-      for (int i = 0; i < L::QF; ++i) {
+      static_for<L::QF>([&](auto I) {
+        constexpr int i = decltype(I)::value;
         C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
         C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
         f[i] = f[i] * (C(1.) - om) + om * eq;
-      }
+      });
     }
   } else {
     C mo[MRT<L::DIM>::K];
-#pragma unroll
-    for (int k = 0; k < MRT<L::DIM>::K; ++k) mo[k] = mrt_moment<L::DIM>(k, f);
+    mrt_moments<L::DIM>(f, mo);
     if (L::DIM == 2)
       mrt2d_relax(mo, rho, jx, jy, p);
     else
@@ -437,6 +733,10 @@ template <int LAT, int COLL, class C>
 __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C dimult, C& dg,
                                              const KParams& p) {
   using L = Lattice<LAT>;
+  if constexpr (LAT == LAT_D3Q19 && COLL == LBM_MRT) {
+    mrt3d_pair_reverse(fin, lam, imult, dimult, dg, p);
+    return;
+  }
   constexpr int QF = L::QF;
   C fo[QF];
 #pragma unroll
@@ -445,7 +745,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
   {
     // base collision output (without PBB), as the reverse PBB recomputes it
     flow_macros<LAT>(fo, rho, jx, jy, jz);
-    const C om = C(p.omega);
+    const C om = mp<C>(p).omega;
     if (COLL == LBM_BGK) {
       if (L::DIM == 2) {
         const C uSqr = jx * jx + jy * jy;
@@ -463,17 +763,16 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
         fo[7] = rel * fo[7] + om * diagW * (cFeq + C(3.) * (jx + jy) + C(4.5) * (uSqr + C(2.) * jx * jy));
       } else {
         const C uSqr = jx * jx + jy * jy + jz * jz;
-#pragma unroll
-        for (int i = 0; i < QF; ++i) {
+        static_for<QF>([&](auto I) {
+          constexpr int i = decltype(I)::value;
           C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
           C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
           fo[i] = fo[i] * (C(1.) - om) + om * eq;
-        }
+        });
       }
     } else {
       C mo[MRT<L::DIM>::K];
-#pragma unroll
-      for (int k = 0; k < MRT<L::DIM>::K; ++k) mo[k] = mrt_moment<L::DIM>(k, fo);
+      mrt_moments<L::DIM>(fo, mo);
       if (L::DIM == 2)
         mrt2d_relax(mo, rho, jx, jy, p);
       else
@@ -493,7 +792,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
   }
   dg += dimult * imultRev;
   // reverse base collision
-  const C om = C(p.omega);
+  const C om = mp<C>(p).omega;
   if (COLL == LBM_BGK) {
     if (L::DIM == 2) {
       const C rel = C(1.) - om;
@@ -551,8 +850,8 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
       lam[8] = li[8] + (r0 + r1);
     } else {
       C rR = C(0.), jR0 = C(0.), jR1 = C(0.), jR2 = C(0.);
-#pragma unroll
-      for (int i = 0; i < QF; ++i) {
+      static_for<QF>([&](auto I) {
+        constexpr int i = decltype(I)::value;
         C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
         C a = om * C(L::w(i)) * lam[i];
         rR += a;
@@ -560,40 +859,42 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
         jR0 += ds * C(L::ex(i)) - C(3.) * a * jx;
         jR1 += ds * C(L::ey(i)) - C(3.) * a * jy;
         jR2 += ds * C(L::ez(i)) - C(3.) * a * jz;
-      }
-#pragma unroll
-      for (int i = 0; i < QF; ++i)
+      });
+      static_for<QF>([&](auto I) {
+        constexpr int i = decltype(I)::value;
         lam[i] = (C(1.) - om) * lam[i] + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) +
                                           jR2 * C(L::ez(i)));
+      });
     }
   } else {
     using M = MRT<L::DIM>;
     C a[M::K];
     C rate[M::K];
     if (L::DIM == 2) {
-      rate[0] = C(p.mrt[0]);
-      rate[1] = C(p.mrt[1]);
-      rate[2] = C(p.mrt[2]);
-      rate[3] = C(p.mrt[2]);
+      rate[0] = mp<C>(p).mrt[0];
+      rate[1] = mp<C>(p).mrt[1];
+      rate[2] = mp<C>(p).mrt[2];
+      rate[3] = mp<C>(p).mrt[2];
       rate[4] = om;
       rate[5] = om;
     } else {
-      rate[0] = C(p.mrt[0]);
-      rate[1] = C(p.mrt[1]);
-      rate[2] = rate[3] = rate[4] = C(p.mrt[2]);
+      rate[0] = mp<C>(p).mrt[0];
+      rate[1] = mp<C>(p).mrt[1];
+      rate[2] = rate[3] = rate[4] = mp<C>(p).mrt[2];
       rate[5] = om;
-      rate[6] = C(p.mrt[3]);
+      rate[6] = mp<C>(p).mrt[3];
       rate[7] = om;
-      rate[8] = C(p.mrt[3]);
+      rate[8] = mp<C>(p).mrt[3];
       rate[9] = rate[10] = rate[11] = om;
-      rate[12] = rate[13] = rate[14] = C(p.mrt[4]);
+      rate[12] = rate[13] = rate[14] = mp<C>(p).mrt[4];
     }
-#pragma unroll
-    for (int k = 0; k < M::K; ++k) {
+    static_for<M::K>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
       // sum_i (-M[k][i]/N_k) lam_i
-      C s = mrt_moment<L::DIM>(k, lam);
-      a[k] = rate[k] * (C(-1.0 / (double)M::n(k)) * s);
-    }
+      C s = mrt_moment<L::DIM, k>(lam);
+      constexpr double inv = -1.0 / (double)M::n(k);
+      a[k] = rate[k] * (C(inv) * s);
+    });
     C rR, jR0, jR1, jR2;
     if (L::DIM == 2) {
       rR = -(a[0] * C(-2.) + a[1]);
@@ -601,7 +902,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
       jR1 = -(a[0] * C(6.) * jy - a[1] * C(6.) * jy - a[3] - a[4] * C(2.) * jy + a[5] * jx);
       jR2 = C(0.);
     } else {
-      const C we = C(p.mrt[5]), wej = C(p.mrt[6]), wxx = C(p.mrt[7]);
+      const C we = mp<C>(p).mrt[5], wej = mp<C>(p).mrt[6], wxx = mp<C>(p).mrt[7];
       const C c2 = C(-2. / 3.);
       const C a56 = a[5] + wxx * a[6], a78 = a[7] + wxx * a[8];
       rR = -(a[0] * C(-11.) + a[1] * we);
@@ -612,17 +913,22 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
       jR2 = -(a[0] * C(38.) * jz + a[1] * C(2.) * wej * jz + a[4] * c2 - a56 * C(2.) * jz -
               a78 * C(2.) * jz + a[10] * jy + a[11] * jx);
     }
-#pragma unroll
-    for (int i = 0; i < QF; ++i) {
+    static_for<QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
       C v = lam[i];
-#pragma unroll
-      for (int k = 0; k < M::K; ++k) {
-        const int c = M::m(k, i);
-        if (c == 0) continue;
-        v += C(c) * a[k];
-      }
+      static_for<M::K>([&](auto KK) {
+        constexpr int k = decltype(KK)::value;
+        constexpr int c = M::m(k, i);
+        if constexpr (c == 1) {
+          v += a[k];
+        } else if constexpr (c == -1) {
+          v -= a[k];
+        } else if constexpr (c != 0) {
+          v += C(c) * a[k];
+        }
+      });
       lam[i] = v + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) + jR2 * C(L::ez(i)));
-    }
+    });
   }
 }
 
@@ -634,7 +940,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
 
 template <class C>
 __device__ __forceinline__ C thermal_omega(C g, const KParams& p) {
-  C imult = C(p.diff) * ramp(g, C(p.ramp_q), C(p.ramp_ck));
+  C imult = mp<C>(p).diff * ramp(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck);
   return C(1.) / (C(3.) * imult + C(0.5));
 }
 
@@ -644,14 +950,14 @@ __device__ __forceinline__ void thermal_collide(C* gp, C ux, C uy, C g, C& T, co
   constexpr int EX5[5] = {0, 0, -1, 0, 1}, EY5[5] = {0, -1, 0, 1, 0};
   const C om = thermal_omega(g, p);
   T = gp[0] + gp[1] + gp[2] + gp[3] + gp[4];
-  const C hs = (C(1.) - g) * C(p.heat_rate) * (C(p.heat_T) - T);
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
+  const C hs = (C(1.) - g) * mp<C>(p).heat_rate * (mp<C>(p).heat_T - T);
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
     C sc = C(EX5[i]) * ux + C(EY5[i]) * uy;
     C eq = C(W5[i]) * T * (C(1.) + C(3.) * sc);
     gp[i] = gp[i] * (C(1.) - om) + om * eq;
     gp[i] += C(W5[i]) * hs;
-  }
+  });
 }
 
 // Transpose of thermal_collide at input (gin, ux, uy); lam[0..4] in/out;
@@ -667,8 +973,8 @@ __device__ __forceinline__ void thermal_reverse(const C* gin, C* lam, C ux, C uy
   uxR = C(0.);
   uyR = C(0.);
   C li[5];
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
     C sc = C(EX5[i]) * ux + C(EY5[i]) * uy;
     C eq = C(W5[i]) * T * (C(1.) + C(3.) * sc);
     li[i] = (C(1.) - om) * lam[i];
@@ -678,11 +984,11 @@ __device__ __forceinline__ void thermal_reverse(const C* gin, C* lam, C ux, C uy
     uxR += a * T * C(3.) * C(EX5[i]);
     uyR += a * T * C(3.) * C(EY5[i]);
     hsR += C(W5[i]) * lam[i];
-  }
-  TR += -(C(1.) - g) * C(p.heat_rate) * hsR;
-  dg += -C(p.heat_rate) * (C(p.heat_T) - T) * hsR;
-  const C den = C(3.) * C(p.diff) * ramp(g, C(p.ramp_q), C(p.ramp_ck)) + C(0.5);
-  dg += omR * (C(-1.) / (den * den)) * C(3.) * C(p.diff) * ramp_diff(g, C(p.ramp_q), C(p.ramp_ck));
+  });
+  TR += -(C(1.) - g) * mp<C>(p).heat_rate * hsR;
+  dg += -mp<C>(p).heat_rate * (mp<C>(p).heat_T - T) * hsR;
+  const C den = C(3.) * mp<C>(p).diff * ramp(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck) + C(0.5);
+  dg += omR * (C(-1.) / (den * den)) * C(3.) * mp<C>(p).diff * ramp_diff(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck);
 #pragma unroll
   for (int i = 0; i < 5; ++i) lam[i] = li[i] + TR;
 }
@@ -692,17 +998,6 @@ __device__ __forceinline__ void thermal_reverse(const C* gin, C* lam, C ux, C uy
 // Zou-He (boundaryConditions/ZouHe2d.hh:23-281), Hecht (Hecht3d.hh:62-94,175-209),
 // thermal Zou-He (thermalZouHe2d.hh:63-81).
 
-__device__ __forceinline__ double bc_profile(const DevBC& b, int y, int z, int ny, int nz, int dim) {
-  if (b.profile != LBM_PROFILE_PARABOLIC) return 1.;
-  double mid = (double)(ny - 1) / 2.;
-  double pr = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
-  if (dim == 3) {
-    double mz = (double)(nz - 1) / 2.;
-    pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
-  }
-  return pr;
-}
-
 template <int LAT, bool SHIFT, class C>
 __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KParams& p) {
   using L = Lattice<LAT>;
@@ -710,9 +1005,9 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
     const DevBC& b = p.bc[k];
     if (!in_box(b.box, x, y, z)) continue;
     if (b.kind == LBM_BC_VELOCITY) {
-      double vv = b.value;
-      vv *= bc_profile(b, y, z, p.ny, p.nz, L::DIM);
-      const C ux = C(vv);
+      // u = value(t) * profile(y, z) (profile tabulated at set-up, see DevBC)
+      C ux = bc_value<C>(b);
+      ux *= bc_prof<C>(b, y, z);
       if (L::DIM == 2) {
         const C uy = C(0.);
         if (b.face == LBM_FACE_WEST) {
@@ -737,7 +1032,7 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
         }
       }
     } else if (b.kind == LBM_BC_PRESSURE) {
-      const C rho0 = SHIFT ? C(b.value - 1.) : C(b.value);
+      const C rho0 = SHIFT ? bc_vshift<C>(b) : bc_value<C>(b);
       if (L::DIM == 2) {
         if (b.face == LBM_FACE_EAST) {
           C ux0 = -rho0 + (f[0] + f[2] + f[6] + C(2.) * (f[1] + f[7] + f[8]));
@@ -764,7 +1059,7 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
     } else if (b.kind == LBM_BC_TEMPERATURE && LAT == LAT_D2Q9_D2Q5) {
       if (b.face == LBM_FACE_WEST) {
         C* g = f + 9;
-        g[4] = C(b.value) - g[0] - g[1] - g[2] - g[3];
+        g[4] = bc_value<C>(b) - g[0] - g[1] - g[2] - g[3];
       }
     }
   }
@@ -863,45 +1158,63 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
 // (temperatureFlow2d.hh:106-142), dissipated power (no reference counterpart):
 // D = 2 alpha |j|^2 + (9/2) nu omega^2 sum_ab Pneq_ab^2.
 
+// component a of e_i
+template <class L>
+__host__ __device__ constexpr int lat_e(int i, int a) {
+  return a == 0 ? L::ex(i) : a == 1 ? L::ey(i) : L::ez(i);
+}
+
+// P_ab = sum_i e_ia e_ib f_i over the flow lattice
+template <int LAT, class C>
+__device__ __forceinline__ void second_moment(const C* f, C (&P)[3][3]) {
+  using L = Lattice<LAT>;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    static_for<L::DIM>([&](auto A) {
+      constexpr int a = decltype(A)::value;
+      static_for<L::DIM>([&](auto B) {
+        constexpr int b = decltype(B)::value;
+        constexpr int eab = lat_e<L>(i, a) * lat_e<L>(i, b);
+        if constexpr (eab == 1) P[a][b] += f[i];
+        if constexpr (eab == -1) P[a][b] -= f[i];
+      });
+    });
+  });
+}
+
+// Weighted objective of one cell, in the compute precision.  On shifted
+// storage the pressure drop sums rho - 1: the constant parts of the inflow and
+// outflow means cancel (weight*1 - weight*1).
 template <int LAT, bool SHIFT, class C>
-__device__ __forceinline__ double objective_cell(const C* f, C g, int x, int y, int z,
-                                                 const KParams& p) {
+__device__ __forceinline__ C objective_cell(const C* f, C g, int x, int y, int z,
+                                            const KParams& p) {
   using L = Lattice<LAT>;
   if (p.objective == LBM_OBJ_PRESSURE_DROP) {
     bool i1 = in_box(p.obj_in, x, y, z), i2 = in_box(p.obj_out, x, y, z);
-    if (!i1 && !i2) return 0.;
+    if (!i1 && !i2) return C(0.);
     C rho, jx, jy, jz;
     flow_macros<LAT>(f, rho, jx, jy, jz);
-    double r = SHIFT ? 1. + (double)rho : (double)rho;
-    double v = 0.;
-    if (i1) v += p.obj_weight * p.inv_in * r;
-    if (i2) v -= p.obj_weight * p.inv_out * r;
+    C v = C(0.);
+    if (i1) v += mp<C>(p).w_in * rho;
+    if (i2) v -= mp<C>(p).w_out * rho;
     return v;
   }
   if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
-    if (!in_box(p.obj_out, x, y, z)) return 0.;
+    if (!in_box(p.obj_out, x, y, z)) return C(0.);
     C rho, jx, jy, jz;
     flow_macros<LAT>(f, rho, jx, jy, jz);
     C T = f[9] + f[10] + f[11] + f[12] + f[13];
-    return -p.obj_weight * (double)jx * (double)T;
+    return -mp<C>(p).obj_weight * jx * T;
   }
   if (p.objective == LBM_OBJ_DISSIPATION) {
     C rho, j[3];
     flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
     C P[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
-#pragma unroll
-    for (int i = 0; i < L::QF; ++i) {
-      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
-#pragma unroll
-      for (int a = 0; a < L::DIM; ++a)
-#pragma unroll
-        for (int b = 0; b < L::DIM; ++b)
-          if (e[a] * e[b] != 0) P[a][b] += C(e[a] * e[b]) * f[i];
-    }
+    second_moment<LAT>(f, P);
     C s2 = C(0.);
 #pragma unroll
     for (int a = 0; a < L::DIM; ++a) {
@@ -912,13 +1225,12 @@ __device__ __forceinline__ double objective_cell(const C* f, C g, int x, int y, 
         s2 += v * v;
       }
     }
-    const double om = p.omega, nu = (1. / om - 0.5) / 3.;
-    const C cv = C(4.5 * nu * om * om);
-    const C alpha = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
+    const C cv = mp<C>(p).cv_diss;
+    const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    return p.obj_weight * (double)(C(2.) * alpha * jj + cv * s2);
+    return mp<C>(p).obj_weight * (C(2.) * alpha * jj + cv * s2);
   }
-  return 0.;
+  return C(0.);
 }
 
 // lam += weight * dF/df ; dg += weight * dF/dgamma
@@ -928,12 +1240,12 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
   using L = Lattice<LAT>;
   if (p.objective == LBM_OBJ_PRESSURE_DROP) {
     if (in_box(p.obj_in, x, y, z)) {
-      const C v = C(p.inv_in * p.obj_weight);
+      const C v = mp<C>(p).w_in;
 #pragma unroll
       for (int d = 0; d < L::QF; ++d) lam[d] += v;
     }
     if (in_box(p.obj_out, x, y, z)) {
-      const C v = C(p.inv_out * p.obj_weight);
+      const C v = mp<C>(p).w_out;
 #pragma unroll
       for (int d = 0; d < L::QF; ++d) lam[d] -= v;
     }
@@ -942,9 +1254,11 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
       C rho, jx, jy, jz;
       flow_macros<LAT>(f, rho, jx, jy, jz);
       C T = f[9] + f[10] + f[11] + f[12] + f[13];
-      const C tc = C(p.obj_weight);
-#pragma unroll
-      for (int d = 0; d < 9; ++d) lam[d] -= tc * C(L::ex(d)) * T;
+      const C tc = mp<C>(p).obj_weight;
+      static_for<9>([&](auto D) {
+        constexpr int d = decltype(D)::value;
+        lam[d] -= tc * C(L::ex(d)) * T;
+      });
 #pragma unroll
       for (int d = 9; d < 14; ++d) lam[d] -= tc * jx;
     }
@@ -952,19 +1266,7 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
     C rho, j[3];
     flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
     C P[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
-#pragma unroll
-    for (int i = 0; i < L::QF; ++i) {
-      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
-#pragma unroll
-      for (int a = 0; a < L::DIM; ++a)
-#pragma unroll
-        for (int b = 0; b < L::DIM; ++b)
-          if (e[a] * e[b] != 0) P[a][b] += C(e[a] * e[b]) * f[i];
-    }
+    second_moment<LAT>(f, P);
     C tr = C(0.);
 #pragma unroll
     for (int a = 0; a < L::DIM; ++a) {
@@ -973,58 +1275,57 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
       P[a][a] -= rho / C(3.);
       tr += P[a][a];
     }
-    const double om = p.omega, nu = (1. / om - 0.5) / 3.;
-    const C cv = C(4.5 * nu * om * om);
-    const C alpha = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
-    const C tc = C(p.obj_weight);
-#pragma unroll
-    for (int i = 0; i < L::QF; ++i) {
-      const int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
+    const C cv = mp<C>(p).cv_diss;
+    const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
+    const C tc = mp<C>(p).obj_weight;
+    static_for<L::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
       C pe = C(0.), pej = C(0.);
 #pragma unroll
       for (int a = 0; a < L::DIM; ++a)
 #pragma unroll
         for (int b = 0; b < L::DIM; ++b) {
-          if (e[a] * e[b] != 0) pe += P[a][b] * C(e[a] * e[b]);
-          if (e[a] != 0) pej += P[a][b] * C(e[a]) * j[b];
+          pe += P[a][b] * C(e[a] * e[b]);
+          pej += P[a][b] * C(e[a]) * j[b];
         }
       C ej = C(e[0]) * j[0] + C(e[1]) * j[1] + C(e[2]) * j[2];
       lam[i] += tc * (C(4.) * alpha * ej + cv * C(2.) * (pe - tr / C(3.) - C(2.) * pej));
-    }
+    });
     C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    dg += tc * (C(2.) * (C(0.5) * (C(p.pbb_scale) * bp_diff(g, C(p.pbb_q)))) * jj);
+    dg += tc * (C(2.) * (C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q))) * jj);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Deterministic block + grid reduction of one double per thread: each block
-// writes its partial, the last block to finish sums the partials in a fixed
-// order and writes *result.
+// Deterministic block + grid reduction of one value per thread: warps sum in
+// the compute precision, per-warp partials are added in FP64, each block
+// writes its FP64 partial, and the last block to finish sums the partials in
+// a fixed order and writes *result.
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
+template <class C>
+__device__ __forceinline__ C warp_sum(C v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-  const int nthr = blockDim.x * blockDim.y;
-  if ((tid & 31) == 0) sh[tid >> 5] = v;
-  __syncthreads();
-  double s = 0.;
-  if (tid < 32) {
-    s = (tid < (nthr + 31) / 32) ? sh[tid] : 0.;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  }
-  return s;   // valid in thread 0
+  return v;
 }
 
-__device__ __forceinline__ void grid_reduce(double v, const KParams& p) {
+template <class C>
+__device__ __forceinline__ void grid_reduce(C v, const KParams& p) {
   __shared__ double sh[32];
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const int nthr = blockDim.x * blockDim.y;
   const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
   const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  double s = block_sum(v, sh);
+  // warps whose cells contribute nothing (e.g. away from the pressure-drop
+  // strips) skip the shuffle tree
+  if (__any_sync(0xffffffffu, v != C(0.))) v = warp_sum(v);
+  if ((tid & 31) == 0) sh[tid >> 5] = (double)v;
+  __syncthreads();
   if (tid == 0) {
+    double s = 0.;
+    for (int w = 0; w < (nthr + 31) / 32; ++w) s += sh[w];
     p.partial[bid] = s;
     __threadfence();
     unsigned prev = atomicAdd(p.counter, 1u);
@@ -1033,12 +1334,15 @@ __device__ __forceinline__ void grid_reduce(double v, const KParams& p) {
   __syncthreads();
   if (!last) return;
   __threadfence();
-  const int nthr = blockDim.x * blockDim.y;
   double acc = 0.;
   for (unsigned i = tid; i < nblk; i += nthr) acc += ((volatile double*)p.partial)[i];
+  acc = warp_sum(acc);
   __syncthreads();
-  double tot = block_sum(acc, sh);
+  if ((tid & 31) == 0) sh[tid >> 5] = acc;
+  __syncthreads();
   if (tid == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (nthr + 31) / 32; ++w) tot += sh[w];
     *p.result = tot;
     *p.counter = 0u;
   }

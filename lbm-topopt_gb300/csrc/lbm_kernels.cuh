@@ -20,6 +20,20 @@
 
 namespace lbm {
 
+// Resident 256-thread blocks per SM requested from the compiler (register
+// cap).  The FP32/FP16 step kernels are HBM-bound and need the warps to keep
+// enough loads in flight: 4 blocks (64 registers) measured fastest for the
+// D3Q19 adjoint; the FP64 kernels are FP64-throughput-bound on GB300 and keep
+// all their registers.
+template <class S>
+struct Occupancy {
+  static constexpr int fwd = 4, adj = 4;
+};
+template <>
+struct Occupancy<double> {
+  static constexpr int fwd = 1, adj = 1;
+};
+
 template <class S>
 struct AdjT {
   using T = S;
@@ -29,45 +43,117 @@ struct AdjT<__half> {
   using T = float;   // FP16 population storage keeps FP32 adjoints
 };
 
-template <int LAT>
-__device__ __forceinline__ long long nb_offset(int q, int nx, int ny) {
+// Offset of the neighbour x + e_q in the SoA index (compile-time q).  All
+// offsets are 32-bit: the host guarantees Q * P < 2^31.
+template <int LAT, int q>
+__device__ __forceinline__ int nb_offset(int sx, int sxy) {
   using L = Lattice<LAT>;
-  return (long long)L::ex(q) + (long long)L::ey(q) * nx + (long long)L::ez(q) * nx * ny;
+  return L::ex(q) + L::ey(q) * sx + L::ez(q) * sxy;
 }
 
-template <int LAT>
-__device__ __forceinline__ bool nb_inside(int q, int x, int y, int z, const KParams& p) {
+template <int LAT, int q>
+__device__ __forceinline__ bool nb_inside(int x, int y, int z, const KParams& p) {
   using L = Lattice<LAT>;
   const int sx = x + L::ex(q), sy = y + L::ey(q), sz = z + L::ez(q);
   return sx >= 0 && sy >= 0 && sz >= 0 && sx < p.nx && sy < p.ny && sz < p.nz;
 }
 
-template <int LAT, class S>
-__device__ __forceinline__ void load_state(typename Store<S>::C* f, const S* fin, long long c,
-                                           long long P) {
+// Cells at least one cell away from every domain face: all neighbours exist.
+template <int LAT>
+__device__ __forceinline__ bool interior(int x, int y, int z, const KParams& p) {
   using L = Lattice<LAT>;
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) f[q] = Store<S>::ld(fin + q * P + c);
+  bool in = x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1;
+  if (L::DIM == 3) in = in && z > 0 && z < p.nz - 1;
+  return in;
+}
+
+// Boundary conditions only live on the x = 0 and x = nx-1 faces (checked
+// when the handle is created), so other cells skip the boundary loop.
+__device__ __forceinline__ bool on_bc_face(int x, const KParams& p) {
+  return p.apply_bc && (x == 0 || x == p.nx - 1);
+}
+
+template <int LAT, class S>
+__device__ __forceinline__ void load_state(typename Store<S>::C* f, const S* __restrict__ fin,
+                                           int c, int P) {
+  using L = Lattice<LAT>;
+  static_for<L::Q>([&](auto Q_) {
+    constexpr int q = decltype(Q_)::value;
+    f[q] = Store<S>::ld(fin + (q * P + c));
+  });
 }
 
 // f~ -> f (unshifted FP64 value of population q)
-template <int LAT, class S>
-__device__ __forceinline__ double to_abs(int q, typename Store<S>::C v) {
+template <int LAT, class S, int q>
+__device__ __forceinline__ double to_abs(typename Store<S>::C v) {
   using L = Lattice<LAT>;
-  return (Store<S>::SHIFT && q < L::QF) ? (double)v + L::w(q) : (double)v;
+  if constexpr (Store<S>::SHIFT && q < L::QF) {
+    return (double)v + L::w(q);
+  } else {
+    return (double)v;
+  }
 }
 
-template <int LAT, class S>
-__device__ __forceinline__ typename Store<S>::C from_abs(int q, double v) {
+template <int LAT, class S, int q>
+__device__ __forceinline__ typename Store<S>::C from_abs(double v) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
-  return (Store<S>::SHIFT && q < L::QF) ? C(v - L::w(q)) : C(v);
+  if constexpr (Store<S>::SHIFT && q < L::QF) {
+    return C(v - L::w(q));
+  } else {
+    return C(v);
+  }
+}
+
+// Push f[q] of cell c to its neighbour (or bounce it back into opp(q) of c).
+// Interior cells take one branch with no per-direction tests.
+template <int LAT, class S>
+__device__ __forceinline__ void push_all(const typename Store<S>::C* f, S* __restrict__ fout,
+                                         int c, int x, int y, int z, bool in, const KParams& p) {
+  using L = Lattice<LAT>;
+  const int P = (int)p.P, sx = p.nx, sxy = p.nx * p.ny;
+  if (in) {
+    static_for<L::Q>([&](auto Q_) {
+      constexpr int q = decltype(Q_)::value;
+      Store<S>::st(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
+    });
+  } else {
+    static_for<L::Q>([&](auto Q_) {
+      constexpr int q = decltype(Q_)::value;
+      if (nb_inside<LAT, q>(x, y, z, p))
+        Store<S>::st(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
+      else
+        Store<S>::st(fout + (L::opp(q) * P + c), f[q]);
+    });
+  }
+}
+
+// Pull lam^post(x, q) = eta(x + e_q, q), or eta(x, opp q) at walls.
+template <int LAT, class A, class C>
+__device__ __forceinline__ void pull_all(C* lam, const A* __restrict__ lin, int c, int x, int y,
+                                         int z, bool in, const KParams& p) {
+  using L = Lattice<LAT>;
+  const int P = (int)p.P, sx = p.nx, sxy = p.nx * p.ny;
+  if (in) {
+    static_for<L::Q>([&](auto Q_) {
+      constexpr int q = decltype(Q_)::value;
+      lam[q] = C(lin[q * P + c + nb_offset<LAT, q>(sx, sxy)]);
+    });
+  } else {
+    static_for<L::Q>([&](auto Q_) {
+      constexpr int q = decltype(Q_)::value;
+      if (nb_inside<LAT, q>(x, y, z, p))
+        lam[q] = C(lin[q * P + c + nb_offset<LAT, q>(sx, sxy)]);
+      else
+        lam[q] = C(lin[L::opp(q) * P + c]);
+    });
+  }
 }
 
 // ---------------------------------------------------------------------------
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256) k_forward(KParams p) {
+__global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
@@ -75,36 +161,30 @@ __global__ void __launch_bounds__(256) k_forward(KParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  double objv = 0.;
+  C objv = C(0.);
   if (x < p.nx && y < p.ny) {
-    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    const int c = (z * p.ny + y) * p.nx + x;
     const S* __restrict__ fin = (const S*)p.fin;
     S* __restrict__ fout = (S*)p.fout;
     C f[L::Q];
-    load_state<LAT, S>(f, fin, c, p.P);
-    if (p.apply_bc) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    load_state<LAT, S>(f, fin, c, (int)p.P);
+    if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     const C g = C(((const G*)p.gamma)[c]);
     if (p.eval_obj) objv = objective_cell<LAT, SHIFT>(f, g, x, y, z, p);
-    const C imult = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
+    const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C rho, jx, jy, jz;
     flow_collide<LAT, COLL>(f, imult, rho, jx, jy, jz, p);
     if (LAT == LAT_D2Q9_D2Q5) {
       C T;
       thermal_collide(f + 9, jx, jy, g, T, p);
     }
-#pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-      if (nb_inside<LAT>(q, x, y, z, p))
-        Store<S>::st(fout + q * p.P + c + nb_offset<LAT>(q, p.nx, p.ny), f[q]);
-      else
-        Store<S>::st(fout + L::opp(q) * p.P + c, f[q]);
-    }
+    push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
   }
   if (p.eval_obj) grid_reduce(objv, p);
 }
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256) k_adjoint(KParams p) {
+__global__ void __launch_bounds__(256, Occupancy<S>::adj) k_adjoint(KParams p) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
@@ -114,23 +194,17 @@ __global__ void __launch_bounds__(256) k_adjoint(KParams p) {
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   const A* __restrict__ lin = (const A*)p.lam_in;
   A* __restrict__ lout = (A*)p.lam_out;
   C lam[L::Q];
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) {
-    if (nb_inside<LAT>(q, x, y, z, p))
-      lam[q] = C(lin[q * p.P + c + nb_offset<LAT>(q, p.nx, p.ny)]);
-    else
-      lam[q] = C(lin[L::opp(q) * p.P + c]);
-  }
+  pull_all<LAT, A, C>(lam, lin, c, x, y, z, interior<LAT>(x, y, z, p), p);
   C f[L::Q];
-  load_state<LAT, S>(f, (const S*)p.fin, c, p.P);
-  if (p.apply_bc) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+  load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
+  if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
   const C g = C(((const G*)p.gamma)[c]);
-  const C imult = C(0.5) * (C(p.pbb_scale) * bp(g, C(p.pbb_q)));
-  const C dimult = C(0.5) * (C(p.pbb_scale) * bp_diff(g, C(p.pbb_q)));
+  const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
+  const C dimult = C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q));
   C dg = C(0.);
   C uxR = C(0.), uyR = C(0.);
   if (LAT == LAT_D2Q9_D2Q5) {
@@ -139,14 +213,18 @@ __global__ void __launch_bounds__(256) k_adjoint(KParams p) {
     thermal_reverse(f + 9, lam + 9, jx, jy, g, uxR, uyR, dg, p);
   }
   flow_reverse<LAT, COLL>(f, lam, imult, dimult, dg, p);
-  if (LAT == LAT_D2Q9_D2Q5) {
-#pragma unroll
-    for (int i = 0; i < 9; ++i) lam[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+  if constexpr (LAT == LAT_D2Q9_D2Q5) {
+    static_for<9>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      lam[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+    });
   }
   if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p);
-  if (p.apply_bc) adjoint_bcs<LAT>(lam, x, y, z, p);
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) lout[q * p.P + c] = A(lam[q]);
+  if (on_bc_face(x, p)) adjoint_bcs<LAT>(lam, x, y, z, p);
+  static_for<L::Q>([&](auto Q_) {
+    constexpr int q = decltype(Q_)::value;
+    lout[q * (int)p.P + c] = A(lam[q]);
+  });
   p.sens[c] += (double)dg;
 }
 
@@ -160,12 +238,12 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  double v = 0.;
+  C v = C(0.);
   if (x < p.nx && y < p.ny) {
-    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    const int c = (z * p.ny + y) * p.nx + x;
     C f[L::Q];
-    load_state<LAT, S>(f, (const S*)p.fin, c, p.P);
-    if (p.apply_bc) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
+    if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     v = objective_cell<LAT, SHIFT>(f, C(((const G*)p.gamma)[c]), x, y, z, p);
   }
   grid_reduce(v, p);
@@ -181,10 +259,10 @@ __global__ void __launch_bounds__(256) k_init(KParams p, const double* __restric
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   double rho = 1., u[3] = {0., 0., 0.}, T = 0.;
   if (mac) {
-    const double* m = mac + c * L::NMAC;
+    const double* m = mac + (long long)c * L::NMAC;
     rho = m[0];
     u[0] = m[1];
     u[1] = m[2];
@@ -195,19 +273,19 @@ __global__ void __launch_bounds__(256) k_init(KParams p, const double* __restric
   const double uSqr = (L::DIM == 3) ? u[0] * u[0] + u[1] * u[1] + u[2] * u[2]
                                     : u[0] * u[0] + u[1] * u[1];
   const double rl = Store<S>::SHIFT ? rho - 1. : rho;
-#pragma unroll
-  for (int i = 0; i < L::QF; ++i) {
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
     double sc = (L::DIM == 3) ? L::ex(i) * u[0] + L::ey(i) * u[1] + L::ez(i) * u[2]
                               : L::ex(i) * u[0] + L::ey(i) * u[1];
     double eq = L::w(i) * (rl + 3. * sc + 4.5 * sc * sc - 1.5 * uSqr);
     Store<S>::st(fo + i * p.P + c, C(eq));
-  }
-  if (LAT == LAT_D2Q9_D2Q5) {
-#pragma unroll
-    for (int i = 9; i < 14; ++i) {
+  });
+  if constexpr (LAT == LAT_D2Q9_D2Q5) {
+    static_for<5>([&](auto I) {
+      constexpr int i = 9 + decltype(I)::value;
       double sc = L::ex(i) * u[0] + L::ey(i) * u[1];
       Store<S>::st(fo + i * p.P + c, C(L::w(i) * T * (1. + 3. * sc)));
-    }
+    });
   }
 }
 
@@ -220,12 +298,14 @@ __global__ void __launch_bounds__(256) k_export(KParams p, double* __restrict__ 
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
-  load_state<LAT, S>(f, (const S*)p.fin, c, p.P);
-  if (p.apply_bc) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) aos[c * L::Q + q] = to_abs<LAT, S>(q, f[q]);
+  load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
+  if (on_bc_face(x, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  static_for<L::Q>([&](auto Q_) {
+    constexpr int q = decltype(Q_)::value;
+    aos[(long long)c * L::Q + q] = to_abs<LAT, S, q>(f[q]);
+  });
 }
 
 template <int LAT, class S>
@@ -235,10 +315,12 @@ __global__ void __launch_bounds__(256) k_import(KParams p, const double* __restr
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   S* fo = (S*)p.fout;
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) Store<S>::st(fo + q * p.P + c, from_abs<LAT, S>(q, aos[c * L::Q + q]));
+  static_for<L::Q>([&](auto Q_) {
+    constexpr int q = decltype(Q_)::value;
+    Store<S>::st(fo + q * p.P + c, from_abs<LAT, S, q>(aos[(long long)c * L::Q + q]));
+  });
 }
 
 // Macros of f_t: rho, jx, jy (, jz | T)
@@ -250,13 +332,13 @@ __global__ void __launch_bounds__(256) k_macros(KParams p, double* __restrict__ 
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
-  load_state<LAT, S>(f, (const S*)p.fin, c, p.P);
-  if (p.apply_bc) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
+  if (on_bc_face(x, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
   C rho, jx, jy, jz;
   flow_macros<LAT>(f, rho, jx, jy, jz);
-  double* m = mac + c * L::NMAC;
+  double* m = mac + (long long)c * L::NMAC;
   m[0] = Store<S>::SHIFT ? 1. + (double)rho : (double)rho;
   m[1] = jx;
   m[2] = jy;
@@ -273,17 +355,14 @@ __global__ void __launch_bounds__(256) k_export_adjoint(KParams p, double* __res
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
-  const long long c = ((long long)z * p.ny + y) * p.nx + x;
+  const int c = (z * p.ny + y) * p.nx + x;
   const A* lin = (const A*)p.lam_in;
-#pragma unroll
-  for (int q = 0; q < L::Q; ++q) {
-    double v;
-    if (nb_inside<LAT>(q, x, y, z, p))
-      v = (double)lin[q * p.P + c + nb_offset<LAT>(q, p.nx, p.ny)];
-    else
-      v = (double)lin[L::opp(q) * p.P + c];
-    aos[c * L::Q + q] = v;
-  }
+  double lam[L::Q];
+  pull_all<LAT, A, double>(lam, lin, c, x, y, z, false, p);
+  static_for<L::Q>([&](auto Q_) {
+    constexpr int q = decltype(Q_)::value;
+    aos[(long long)c * L::Q + q] = lam[q];
+  });
 }
 
 template <class G>

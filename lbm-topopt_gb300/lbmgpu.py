@@ -167,7 +167,7 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("LBMGPU_LIBRARY") or LIB_PATH
     if not os.path.exists(p):
         raise OSError("liblbmgpu.so not built at %s (run __graft_entry__.build())" % p)
     lib = C.CDLL(p)
@@ -194,6 +194,8 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_time_steps": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
         "lbm_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
         "lbm_select_device": (C.c_int, [C.c_int]),
+        "lbm_autotune": (C.c_int, [H, C.c_int]),
+        "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
@@ -329,6 +331,16 @@ class Handle:
         ms = C.c_float()
         self._check(self.lib.lbm_time_steps(self.h, int(which), int(nsteps), C.byref(ms)))
         return ms.value
+
+    def autotune(self, nsteps: int = 5):
+        """Pick the fastest thread-block shapes for the step kernels."""
+        self._check(self.lib.lbm_autotune(self.h, int(nsteps)))
+        return self.launch_shape(0), self.launch_shape(1)
+
+    def launch_shape(self, which: int):
+        bx, by = C.c_int(), C.c_int()
+        self._check(self.lib.lbm_get_launch_shape(self.h, int(which), C.byref(bx), C.byref(by)))
+        return bx.value, by.value
 
     def launch_count(self) -> int:
         n = C.c_int64()

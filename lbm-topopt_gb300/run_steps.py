@@ -44,11 +44,14 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, default=None, help="nx ny nz (workload 3)")
     ap.add_argument("--fwd", type=int, default=10)
     ap.add_argument("--adj", type=int, default=10)
+    ap.add_argument("--autotune", action="store_true", help="pick block shapes first")
     a = ap.parse_args()
     cfg, gamma, _ = build_workload(a.workload, STORAGE[a.storage], a.size)
     with G.Handle(cfg) as h:
         h.set_design(gamma)
         h.init_equilibrium()
+        if a.autotune:
+            print("block shapes (forward, reverse):", h.autotune())
         ms_f = h.time_steps(0, a.fwd) if a.fwd > 0 else 0.0
         ms_a = h.time_steps(1, a.adj) if a.adj > 0 else 0.0
         n = cfg.ncells
