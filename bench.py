@@ -313,10 +313,13 @@ def main():
     ach_adj = b_adj / t_adj / 1e9
     ach_fwd = b_fwd / t_fwd / 1e9
     traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    tr_path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if os.path.exists(tr_path):
         with open(tr_path) as f:
-            traffic = json.load(f).get("k_adjoint_fp32_256x128x128_bytes_per_launch")
+            for ln in f:
+                parts = ln.split()
+                if len(parts) == 2 and parts[0] == "k_adjoint_fp32_256x128x128":
+                    traffic = int(parts[1])
 
     # end to end through the C ABI with host buffers: design upload, full checkpointed
     # gradient (5000 steps, 64 device snapshots), sensitivity download
