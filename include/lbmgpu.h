@@ -241,6 +241,33 @@ int lbm_get_launch_count(const lbm_handle* h, int64_t* launches);
  * (WangCheckpointing.cc:72-162 with DynamicCheckpointing.cc:9-54). */
 int lbm_wang_recompute_count(int nsteps, int nsnapshots, int64_t* recomputed);
 
+/* Objective weight*F(f_t) of a state that lives in the caller's own device
+ * memory, computed without allocating any device memory.  For callers that
+ * cannot call cudaMalloc: an application that reserves all of its device
+ * memory up front and forbids later allocations, a real-time loop that cannot
+ * pay cudaMalloc's latency and implicit synchronisation, a process held to a
+ * fixed device-memory budget.  No counterpart in the reference.
+ *   cfg       lattice, storage, boundaries and objective (as for lbm_create)
+ *   t         time step of the state (boundary conditions of step t are applied
+ *             on load when t >= 1)
+ *   f_dev     populations in the handle layout: Q planes of P = ncells rounded
+ *             up to 128 elements, storage precision of cfg (FP32/FP16 planes of
+ *             the flow lattice hold f_i - w_i)
+ *   gamma_dev design, ncells values: double for LBM_STORE_FP64, float otherwise
+ *   J_dev     device address of one double receiving the objective
+ *   stream    cudaStream_t to run on (NULL: the default stream); the result is
+ *             ready when the stream is.
+ * Its scratch (block partial sums, a counter, inflow-profile tables) is one
+ * fixed 640 KiB array per GPU, held for the life of the process.  Limits:
+ * at most 8,388,608 cells and 32,768 tabulated inflow-profile values; larger
+ * requests return LBM_ERR_ARG.  Every call shares that array, so calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address; make that call before any stream capture.
+ * Errors are reported through lbm_last_error(NULL). */
+int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f_dev,
+                          const void* gamma_dev, double* J_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -383,6 +383,11 @@ int init_state(lbm_handle* h) {
 
 }  // namespace
 
+namespace lbm {
+void set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+int validate_config(const lbm_config& c) { return validate(c); }
+}  // namespace lbm
+
 // ===========================================================================
 
 extern "C" {

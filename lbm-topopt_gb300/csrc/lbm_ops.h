@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/lbmgpu.h"
+
 namespace lbm {
 
 struct KParams;
@@ -25,5 +27,10 @@ typedef void (*LaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st, const
 LaunchFn launcher_d2q9(int collision, int storage);
 LaunchFn launcher_d3q19(int collision, int storage);
 LaunchFn launcher_thermal(int collision, int storage);
+
+// Text returned by lbm_last_error(NULL) (errors raised outside a handle).
+void set_global_error(const char* msg);
+// The checks of lbm_create (message through lbm_last_error(NULL)); 0 = valid.
+int validate_config(const lbm_config& c);
 
 }  // namespace lbm
