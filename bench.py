@@ -121,43 +121,59 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def dist_setup():
+def dist_setup(init=True):
+    """One process per GPU (torchrun env).  NCCL with GPUs, gloo without."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
-    if world > 1:
+    if world > 1 and init:
         import torch
         import torch.distributed as td
-        torch.cuda.set_device(local)
-        td.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            td.init_process_group("nccl")
+        else:
+            td.init_process_group("gloo")
         dist = td
     return world, rank, local, dist
 
 
+def _on_gpu(dist):
+    return dist is not None and dist.get_backend() == "nccl"
+
+
 def barrier(dist):
     if dist is not None:
-        import torch
         dist.barrier()
-        torch.cuda.synchronize()
+        if _on_gpu(dist):
+            import torch
+            torch.cuda.synchronize()
+
+
+def _reduce(dist, v, op):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device="cuda" if _on_gpu(dist) else "cpu")
+    dist.all_reduce(t, op=op)
+    return float(t.item())
 
 
 def max_over_ranks(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([float(v)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return _reduce(dist, v, dist.ReduceOp.MAX) if dist is not None else v
 
 
 def sum_over_ranks(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([float(v)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(dist, v, dist.ReduceOp.SUM) if dist is not None else v
+
+
+def aggregate_mlups(dist, cells, steps, ms):
+    """Whole-job throughput of independent replicas: all ranks' lattice updates
+    over the slowest rank's device time."""
+    total = sum_over_ranks(dist, cells * steps)
+    slowest = max_over_ranks(dist, ms)
+    return total / (slowest * 1e-3) / 1e6, slowest
 
 
 # ----------------------------------------------------------------------------------------
@@ -270,10 +286,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    world, rank, local, dist = dist_setup()
     if args.impl == "reference":
-        reference_arm(args, world, rank)
+        world, rank, _, _ = dist_setup(init=False)
+        reference_arm(args, world, rank)   # rank 0 only; the others exit without work
         return
+    world, rank, local, dist = dist_setup()
 
     import lbmgpu as G
     import workloads as W
@@ -298,11 +315,10 @@ def main():
     ms_fwd = h.time_steps(0, args.steps)
     ms_adj = h.time_steps(1, args.steps)
     clocks = sampler.stop()
-    ms_pairs = max_over_ranks(dist, ms_pairs)
+    value, ms_pairs = aggregate_mlups(dist, cells, args.steps, ms_pairs)
     ms_fwd = max_over_ranks(dist, ms_fwd)
     ms_adj = max_over_ranks(dist, ms_adj)
     total_cells = sum_over_ranks(dist, cells)
-    value = total_cells * args.steps / (ms_pairs * 1e-3) / 1e6
 
     # roofline of the dominant kernel (the adjoint step)
     peak, peak_kind = load_peaks()

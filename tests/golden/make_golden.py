@@ -1,0 +1,75 @@
+"""Generate the golden vectors in this directory from the reference's own
+operators, loops and checkpoint schedule (oracle/_ref/libref.so, built from the
+reference sources by `make -C oracle ref`).  The reference has no tests or
+stored results of its own; these fixtures are its outputs on seeded inputs.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "lbm-topopt_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import lbmgpu as G  # noqa: E402
+import workloads as W  # noqa: E402
+from oracle_lib import reference  # noqa: E402
+
+
+def cases():
+    return {
+        "d2q9_bgk": (W.channel_2d(32, 16, amp=0.2, period=25.0, nsteps=120),
+                     W.design_2d(32, 16, 101), 120),
+        "d2q9_mrt": (W.channel_2d(24, 12, collision=G.MRT, nsteps=80), W.design_2d(24, 12, 102), 80),
+        "d3q19_mrt": (W.duct_3d(16, 8, 8, nsteps=50), W.design_3d(16, 8, 8, 103), 50),
+        "d3q19_mrt_default_rates": (W.duct_3d(12, 8, 8, nsteps=30).replace(mrt=G.MRT3D_DEFAULT),
+                                    W.design_3d(12, 8, 8, 104), 30),
+    }
+
+
+def cell_inputs(cfg, rng, n=16):
+    base = {G.D2Q9: [4 / 9] + [1 / 36, 1 / 9] * 4,
+            G.D3Q19: [1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6}[cfg.lattice]
+    fin = np.array(base)[None, :] * (1 + 0.05 * rng.standard_normal((n, len(base))))
+    g = rng.uniform(0.02, 0.98, n)
+    lo = rng.standard_normal((n, len(base)))
+    return fin, g, lo
+
+
+def main():
+    ref = reference()
+    if ref is None:
+        raise SystemExit("build the reference checker first: make -C oracle ref")
+    rng = np.random.default_rng(20261203)
+    for name, (cfg, gamma, n) in cases().items():
+        f, js, J = ref.forward(cfg, gamma, n)
+        Jg, sens = ref.gradient(cfg, gamma, n)
+        fin, g, lo = cell_inputs(cfg, rng)
+        fout = np.zeros_like(fin)
+        mac = np.zeros((len(g), cfg.nmac))
+        lin = np.zeros_like(fin)
+        dg = np.zeros(len(g))
+        for k in range(len(g)):
+            fout[k], mac[k] = ref.collide_cell(cfg, fin[k], g[k])
+            lin[k], dg[k] = ref.reverse_cell(cfg, fin[k], g[k], lo[k])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), gamma=gamma, nsteps=n, f=f,
+                            J_steps=js, J=J, J_grad=Jg, sens=sens, cell_fin=fin, cell_gamma=g,
+                            cell_fout=fout, cell_mac=mac, cell_lam_out=lo, cell_lam_in=lin,
+                            cell_dgamma=dg)
+        print(name, "J", J, "max|sens|", np.abs(sens).max())
+    table = []
+    for N in (1, 2, 3, 10, 50, 100, 777, 1000, 2000, 4000, 5000, 10000, 20000):
+        for K in (2, 3, 7, 16, 20, 64):
+            r, ok = ref.wang_count(N, K)
+            table.append((N, K, r, int(ok)))
+    np.savetxt(os.path.join(HERE, "wang_schedule.txt"), np.array(table, dtype=np.int64), fmt="%d",
+               header="nsteps nsnapshots recomputed_steps reversal_exact (reference WangCheckpointing + DynamicCheckpointing)")
+    print("wang table", len(table))
+
+
+if __name__ == "__main__":
+    main()
