@@ -82,6 +82,7 @@ extern "C" {
 #define LBM_OBJ_PRESSURE_DROP 1  /* functionals/pressureDrop2d.hh:9-70 */
 #define LBM_OBJ_DISSIPATION   2  /* porous + viscous dissipated power (no reference counterpart) */
 #define LBM_OBJ_HEAT_FLUX     3  /* functionals/temperatureFlow2d.hh:10-63 */
+#define LBM_OBJ_OUTFLOW       4  /* -(mean u_x over obj_out): functionals/outflow2d.hh:10-54 */
 
 typedef struct lbm_bc {
   int kind;        /* LBM_BC_* */

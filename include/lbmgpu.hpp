@@ -1,0 +1,125 @@
+// lbmgpu.hpp -- header-only C++ facade over the C ABI of lbmgpu.h that keeps
+// the method names of the reference's solver classes, so a reference-style
+// driver (applications/RobustPump2d/robustPump2d.cc:234-276) ports by
+// swapping types:
+//
+//   IsothermalLBSolver2d<Op>          -> lbmgpu::IsothermalLBSolver
+//     (latticeBoltzmann/isothermalLBSolver2d.hh:20-110, LBSolver.hh:14-73)
+//   AdjointLBSolver                   -> lbmgpu::AdjointLBSolver
+//     (adjointLatticeBoltzmann/adjointLBSolver.hh:11-46)
+//   LBDynamicCheckpointing            -> lbmgpu::LBDynamicCheckpointing
+//     (topOpt/LBCheckpointing.hh:20-29)
+//
+// Errors come back as the ABI's int status (0 = ok), the role PetscErrorCode
+// plays in the reference; lastError() gives the text.
+#ifndef LBMGPU_HPP
+#define LBMGPU_HPP
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lbmgpu.h"
+
+namespace lbmgpu {
+
+class IsothermalLBSolver {
+ public:
+  IsothermalLBSolver() = default;
+  IsothermalLBSolver(const IsothermalLBSolver&) = delete;
+  IsothermalLBSolver& operator=(const IsothermalLBSolver&) = delete;
+  ~IsothermalLBSolver() { lbm_destroy(h_); }
+
+  // make(comm, info, op) + addBoundaryCondition(...) of the reference: the
+  // whole set-up is one config.
+  int make(const lbm_config& cfg) {
+    lbm_destroy(h_);
+    h_ = nullptr;
+    int rc = lbm_create(&cfg, &h_);
+    if (rc == LBM_OK) lbm_get_sizes(h_, &ncells_, &npop_);
+    return rc;
+  }
+  // LBSolver::setFieldFromDesignVec (LBSolver.cc:333-348)
+  int setFieldFromDesignVec(const std::vector<double>& gamma) {
+    if ((int64_t)gamma.size() != ncells_) return LBM_ERR_ARG;
+    return lbm_set_design(h_, gamma.data());
+  }
+  // LBSolver::initializeAtEquilibrium (LBSolver.cc:234-249); macros empty = rest
+  int initializeAtEquilibrium(const std::vector<double>& macros = {}) {
+    return lbm_init_equilibrium(h_, macros.empty() ? nullptr : macros.data());
+  }
+  // collide() + stream() (LBSolver.cc:163-206) n times, with the objective of
+  // every new state summed into *value (computeMacroFunctional, LBSolver.cc:74-91)
+  int collideAndStream(int n = 1, double* value = nullptr) {
+    return lbm_forward(h_, n, nullptr, value);
+  }
+  int getCurrentTimestep(int* t) const { return lbm_get_time(h_, t); }
+  int getDistributions(std::vector<double>* f) const {
+    f->resize((size_t)ncells_ * npop_);
+    return lbm_get_populations(h_, f->data());
+  }
+  // LBSolver::setDistributions + setCurrentTimestep (LBSolver.cc:65-97)
+  int setDistributions(const std::vector<double>& f, int t) {
+    if ((int64_t)f.size() != ncells_ * npop_) return LBM_ERR_ARG;
+    return lbm_set_populations(h_, f.data(), t);
+  }
+  int getMacros(std::vector<double>* mac, int nmac) const {
+    mac->resize((size_t)ncells_ * nmac);
+    return lbm_get_macros(h_, mac->data());
+  }
+  int autotune(int nsteps = 5) { return lbm_autotune(h_, nsteps); }
+  std::string lastError() const { return lbm_last_error(h_); }
+  lbm_handle* handle() const { return h_; }
+  int64_t numCells() const { return ncells_; }
+  int numPopulations() const { return npop_; }
+
+ private:
+  lbm_handle* h_ = nullptr;
+  int64_t ncells_ = 0;
+  int npop_ = 0;
+};
+
+// The reverse sweep works on the forward solver's handle: its state is the
+// f_t the reverse step differentiates (getForwardSolution places it there).
+class AdjointLBSolver {
+ public:
+  explicit AdjointLBSolver(IsothermalLBSolver& s) : s_(s) {}
+  // AdjointLBSolver::resetAdjoints (adjointLBSolver.cc:138-145)
+  int resetAdjoints() { return lbm_adjoint_reset(s_.handle()); }
+  // adjointCollide + computeCollideSource + computeSensitivitySource +
+  // adjointStream (adjointLBSolver.cc:28-122) at the state held by the solver
+  int adjointStep() { return lbm_adjoint_step(s_.handle()); }
+  // AdjointLBSolver::getSensitivities (adjointLBSolver.cc:153-157)
+  int getSensitivities(std::vector<double>* sens) const {
+    sens->resize((size_t)s_.numCells());
+    return lbm_get_sensitivity(s_.handle(), sens->data());
+  }
+  int getAdjoints(std::vector<double>* lam) const {
+    lam->resize((size_t)s_.numCells() * s_.numPopulations());
+    return lbm_get_adjoint(s_.handle(), lam->data());
+  }
+
+ private:
+  IsothermalLBSolver& s_;
+};
+
+// Forward sweep with Wang et al. dynamic checkpointing in device memory, the
+// reverse sweep, and dJ/dgamma: the driver loop of robustPump2d.cc:234-276
+// with LBDynamicCheckpointing as one call.
+class LBDynamicCheckpointing {
+ public:
+  LBDynamicCheckpointing(int numCheckpoints, IsothermalLBSolver& s) : k_(numCheckpoints), s_(s) {}
+  int objectiveAndGradient(int numSteps, double* J, std::vector<double>* sens,
+                           lbm_gradient_stats* stats = nullptr) {
+    sens->resize((size_t)s_.numCells());
+    return lbm_gradient(s_.handle(), numSteps, k_, J, sens->data(), stats);
+  }
+
+ private:
+  int k_;
+  IsothermalLBSolver& s_;
+};
+
+}  // namespace lbmgpu
+
+#endif  // LBMGPU_HPP

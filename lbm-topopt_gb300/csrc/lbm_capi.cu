@@ -173,6 +173,9 @@ int validate(const lbm_config& c) {
       return fail(nullptr, LBM_ERR_SUP, "heat flux objective needs the thermal lattice");
     int rc = check_box(c, c.obj_out, dim, "objective outflow");
     if (rc) return rc;
+  } else if (c.objective == LBM_OBJ_OUTFLOW) {
+    int rc = check_box(c, c.obj_out, dim, "objective outflow");
+    if (rc) return rc;
   } else if (c.objective != LBM_OBJ_NONE && c.objective != LBM_OBJ_DISSIPATION) {
     return fail(nullptr, LBM_ERR_ARG, "unknown objective %d", c.objective);
   }
@@ -256,8 +259,10 @@ KParams base_params(const lbm_handle* h, int t) {
   }
   if (c.objective == LBM_OBJ_PRESSURE_DROP) {
     const int* a = c.obj_in;
-    const int* b = c.obj_out;
     p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
+  }
+  if (c.objective == LBM_OBJ_PRESSURE_DROP || c.objective == LBM_OBJ_OUTFLOW) {
+    const int* b = c.obj_out;
     p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
   }
   ModelParams<double>& md = p.md;

@@ -1203,6 +1203,12 @@ __device__ __forceinline__ C objective_cell(const C* f, C g, int x, int y, int z
     if (i2) v -= mp<C>(p).w_out * rho;
     return v;
   }
+  if (p.objective == LBM_OBJ_OUTFLOW) {
+    if (!in_box(p.obj_out, x, y, z)) return C(0.);
+    C rho, jx, jy, jz;
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    return -mp<C>(p).w_out * jx;
+  }
   if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
     if (!in_box(p.obj_out, x, y, z)) return C(0.);
     C rho, jx, jy, jz;
@@ -1248,6 +1254,15 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
       const C v = mp<C>(p).w_out;
 #pragma unroll
       for (int d = 0; d < L::QF; ++d) lam[d] -= v;
+    }
+  } else if (p.objective == LBM_OBJ_OUTFLOW) {
+    if (in_box(p.obj_out, x, y, z)) {
+      const C v = mp<C>(p).w_out;
+      static_for<L::QF>([&](auto D) {
+        constexpr int d = decltype(D)::value;
+        if constexpr (L::ex(d) == 1) lam[d] -= v;
+        if constexpr (L::ex(d) == -1) lam[d] += v;
+      });
     }
   } else if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
     if (in_box(p.obj_out, x, y, z)) {

@@ -137,8 +137,10 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
   }
   if (c.objective == LBM_OBJ_PRESSURE_DROP) {
     const int* a = c.obj_in;
-    const int* b = c.obj_out;
     p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
+  }
+  if (c.objective == LBM_OBJ_PRESSURE_DROP || c.objective == LBM_OBJ_OUTFLOW) {
+    const int* b = c.obj_out;
     p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
   }
   md.w_in = p.inv_in * c.obj_weight;

@@ -37,7 +37,7 @@ STORE_FP64, STORE_FP32, STORE_FP16 = 0, 1, 2
 BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE = 1, 2, 3
 FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
 PROFILE_UNIFORM, PROFILE_PARABOLIC = 0, 1
-OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX = 0, 1, 2, 3
+OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX, OBJ_OUTFLOW = 0, 1, 2, 3, 4
 MAX_BC = 8
 
 STATUS_TEXT = {0: "ok", -1: "bad argument", -2: "unsupported", -3: "CUDA error",

@@ -1042,6 +1042,19 @@ static double objective(const model_t* m, const double* F, const double* gamma) 
           ps -= tc * invOut * mac[0];
         }
     return ps;
+  } else if (c->objective == LBM_OBJ_OUTFLOW) {
+    /* OutflowEast2d::evaluate (functionals/outflow2d.hh:15-27) */
+    double invOut = (double)(1. / box_count(c->obj_out));
+    double of = 0.;
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double mac[4];
+          flow_macros(m, F + (((int64_t)z * m->ny + y) * m->nx + x) * Q, mac);
+          of -= tc * invOut * mac[1];
+        }
+    return of;
   } else if (c->objective == LBM_OBJ_HEAT_FLUX) {
     double pout = 0.;
     const int* b = c->obj_out;
@@ -1086,6 +1099,16 @@ static void objective_source(const model_t* m, const double* F, const double* ga
         for (int x = b[0]; x <= b[1]; ++x) {
           double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
           for (int d = 0; d < m->Qf; ++d) a[d] -= invOut * tc;
+        }
+  } else if (c->objective == LBM_OBJ_OUTFLOW) {
+    /* OutflowEast2d::adjointCollideSource, incompressible macros (outflow2d.hh:28-40) */
+    double invOut = (double)(1. / box_count(c->obj_out));
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
+          for (int d = 0; d < m->Qf; ++d) a[d] -= invOut * tc * m->L->ex[d];
         }
   } else if (c->objective == LBM_OBJ_HEAT_FLUX) {
     const int* b = c->obj_out;

@@ -207,6 +207,13 @@ struct Sim2d {
 
   double functional(const std::vector<double>& mac) {
     double tc = c.obj_weight, ps = 0.;
+    if (c.objective == LBM_OBJ_OUTFLOW) {
+      double inv = box_inv(c.obj_out), of = 0.;
+      for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
+        for (int i = c.obj_out[0]; i <= c.obj_out[1]; ++i)
+          of -= tc * inv * mac[((size_t)j * nx + i) * 3 + 1];
+      return of;
+    }
     if (c.objective != LBM_OBJ_PRESSURE_DROP) return 0.;
     double invIn = box_inv(c.obj_in), invOut = box_inv(c.obj_out);
     for (int j = c.obj_in[2]; j <= c.obj_in[3]; ++j)
@@ -219,6 +226,13 @@ struct Sim2d {
   }
 
   void source(std::vector<double>& adj) {
+    if (c.objective == LBM_OBJ_OUTFLOW) {
+      double tc = c.obj_weight, inv = box_inv(c.obj_out);
+      for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
+        for (int i = c.obj_out[0]; i <= c.obj_out[1]; ++i)
+          for (int d = 0; d < 9; ++d) adj[((size_t)j * nx + i) * 9 + d] -= inv * tc * D2Q9::ex[d];
+      return;
+    }
     if (c.objective != LBM_OBJ_PRESSURE_DROP) return;
     double tc = c.obj_weight, invIn = box_inv(c.obj_in), invOut = box_inv(c.obj_out);
     for (int j = c.obj_in[2]; j <= c.obj_in[3]; ++j)

@@ -25,6 +25,8 @@ def cases():
         "d2q9_bgk": (W.channel_2d(32, 16, amp=0.2, period=25.0, nsteps=120),
                      W.design_2d(32, 16, 101), 120),
         "d2q9_mrt": (W.channel_2d(24, 12, collision=G.MRT, nsteps=80), W.design_2d(24, 12, 102), 80),
+        "d2q9_bgk_outflow": (W.channel_2d(28, 14, nsteps=90).replace(objective=G.OBJ_OUTFLOW),
+                             W.design_2d(28, 14, 105), 90),
         "d3q19_mrt": (W.duct_3d(16, 8, 8, nsteps=50), W.design_3d(16, 8, 8, 103), 50),
         "d3q19_mrt_default_rates": (W.duct_3d(12, 8, 8, nsteps=30).replace(mrt=G.MRT3D_DEFAULT),
                                     W.design_3d(12, 8, 8, 104), 30),
