@@ -32,6 +32,7 @@ extern "C" {
 
 #define LBMGPU_ABI_VERSION 1
 #define LBM_MAX_BC 8
+#define LBM_MAX_BATCH 8   /* lattices advanced by one batched launch */
 
 /* Status codes.  PETSc's PetscErrorCode is 0 = ok; the reference's
  * "unsupported" case (PETSC_ERR_SUP, boundaryConditions/LBBoundaryLoop.cc:32-38)
@@ -241,6 +242,39 @@ int lbm_get_launch_count(const lbm_handle* h, int64_t* launches);
  * steps needed to reverse nsteps steps with nsnapshots slots
  * (WangCheckpointing.cc:72-162 with DynamicCheckpointing.cc:9-54). */
 int lbm_wang_recompute_count(int nsteps, int nsnapshots, int64_t* recomputed);
+
+/* ------------------------------------------------------------------------
+ * Batches.  Up to LBM_MAX_BATCH lattices with the same lattice type, collision
+ * and storage (sizes, boundaries, designs and objectives free) advanced
+ * together: one launch per time step covers every lattice, a persistent grid of
+ * resident blocks striding over their concatenated blocks.  The one-GPU form of
+ * the reference's robust-design ensembles (core/MPISplit.cc:14-59,
+ * applications/RobustPump2d/robustPump2d.cc:140-146), where each realisation
+ * ran on its own MPI sub-communicator. */
+typedef struct lbm_batch lbm_batch;
+
+int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* b);
+const char* lbm_batch_last_error(const lbm_batch* b);
+/* The handle of lattice i (owned by the batch): set its design, read its state
+ * and sensitivities with the single-lattice entry points. */
+int lbm_batch_handle(lbm_batch* b, int i, lbm_handle** h);
+/* Pick the block shape of the batched step kernels (states are re-initialised). */
+int lbm_batch_autotune(lbm_batch* b, int nsteps);
+int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by);
+/* nsteps forward steps of every lattice from its current state; J[i] (may be
+ * NULL) gets lattice i's objective sum as lbm_forward would. */
+int lbm_batch_forward(lbm_batch* b, int nsteps, double* J);
+/* lbm_gradient for every lattice at once (same nsteps and nsnapshots).  With
+ * use_graph the whole sequence (initialisation, forward sweep, checkpoint
+ * copies, recomputation, reverse sweep) is captured once as a CUDA graph and
+ * replayed by later calls with the same nsteps and nsnapshots.  J (n values)
+ * and dJdgamma (n pointers, entries may be NULL) may be NULL. */
+int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnapshots, int use_graph, double* J,
+                       double* const* dJdgamma, lbm_gradient_stats* stats);
+/* As lbm_time_steps, for the batched kernels. */
+int lbm_batch_time_steps(lbm_batch* b, int which, int nsteps, float* ms);
+int lbm_batch_get_launch_count(const lbm_batch* b, int64_t* launches);
 
 /* Objective weight*F(f_t) of a state that lives in the caller's own device
  * memory, computed without allocating any device memory.  For callers that

@@ -16,6 +16,35 @@ LaunchFn launcher_d3q19(int collision, int storage) {
   }
   return nullptr;
 }
+
+BatchOps batch_ops_d3q19(int collision, int storage) {
+  BatchOps o;
+  if (collision == LBM_BGK && storage == LBM_STORE_FP64) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, double>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, double>::kernel_address;
+  }
+  if (collision == LBM_BGK && storage == LBM_STORE_FP32) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, float>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, float>::kernel_address;
+  }
+  if (collision == LBM_BGK && storage == LBM_STORE_FP16) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, __half>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, __half>::kernel_address;
+  }
+  if (collision == LBM_MRT && storage == LBM_STORE_FP64) {
+    o.launch = &OpsImpl<LAT, LBM_MRT, double>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_MRT, double>::kernel_address;
+  }
+  if (collision == LBM_MRT && storage == LBM_STORE_FP32) {
+    o.launch = &OpsImpl<LAT, LBM_MRT, float>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_MRT, float>::kernel_address;
+  }
+  if (collision == LBM_MRT && storage == LBM_STORE_FP16) {
+    o.launch = &OpsImpl<LAT, LBM_MRT, __half>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_MRT, __half>::kernel_address;
+  }
+  return o;
+}
 #undef LAT
 
 }  // namespace lbm

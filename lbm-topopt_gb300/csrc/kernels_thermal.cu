@@ -11,6 +11,19 @@ LaunchFn launcher_thermal(int collision, int storage) {
   }
   return nullptr;
 }
+
+BatchOps batch_ops_thermal(int collision, int storage) {
+  BatchOps o;
+  if (collision == LBM_BGK && storage == LBM_STORE_FP64) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, double>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, double>::kernel_address;
+  }
+  if (collision == LBM_BGK && storage == LBM_STORE_FP32) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, float>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, float>::kernel_address;
+  }
+  return o;
+}
 #undef LAT
 
 }  // namespace lbm

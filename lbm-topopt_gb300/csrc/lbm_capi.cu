@@ -936,3 +936,538 @@ int lbm_wang_recompute_count(int nsteps, int nsnap, int64_t* recomputed) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Batches: several lattices (uneven sizes, own boundaries, designs and
+// objectives; same lattice type, collision and storage) advanced together, one
+// launch per time step, with the whole checkpointed gradient optionally
+// captured in a CUDA graph and replayed.  This is the one-GPU form of the
+// reference's MPISplit ensembles (core/MPISplit.cc:14-59: one realisation per
+// sub-communicator) plus uneven extra instances.
+
+namespace {
+
+struct CopyBatch {
+  int n;
+  const uint4* src[LBM_MAX_BATCH];
+  uint4* dst[LBM_MAX_BATCH];
+  long long nvec[LBM_MAX_BATCH];   // 16-byte vectors per buffer
+};
+
+// dst_i <- src_i for every buffer of the batch, 16 bytes per thread and step.
+__global__ void __launch_bounds__(256) k_copy_batch(const __grid_constant__ CopyBatch cb) {
+  for (int i = 0; i < cb.n; ++i) {
+    const uint4* __restrict__ s = cb.src[i];
+    uint4* __restrict__ d = cb.dst[i];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < cb.nvec[i];
+         k += (long long)gridDim.x * blockDim.x)
+      d[k] = s[k];
+  }
+}
+
+}  // namespace
+
+struct lbm_batch {
+  int n = 0;
+  lbm_handle* h[LBM_MAX_BATCH] = {};
+  BatchOps ops;
+  cudaStream_t stream = nullptr;
+  int bx = 128, by = 2;
+  int nsm = 1;
+  int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = -1, graph_snap = -1;
+  int64_t graph_recomputed = 0;
+  int64_t graph_launches = 0;            // kernels in the captured sequence
+  int end_cur[LBM_MAX_BATCH] = {}, end_lcur[LBM_MAX_BATCH] = {};   // host state after it
+  int64_t launches = 0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::string err;
+};
+
+namespace {
+
+int bfail(lbm_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b)
+    b->err = buf;
+  else
+    g_create_error = buf;
+  return code;
+}
+
+#define BCUDA(b, call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return bfail((b), LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Persistent grid: resident blocks of kernel `kind` times SMs, at most the work.
+int batch_grid(lbm_batch* b, int kind, int total) {
+  int per_sm = 1;
+  const void* k = b->ops.kernel(kind);
+  if (k) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, b->bx * b->by, 0);
+  if (per_sm < 1) per_sm = 1;
+  int g = per_sm * b->nsm;
+  return g < total ? g : total;
+}
+
+void batch_layout(lbm_batch* b, BatchParams& bp) {
+  bp.n = b->n;
+  int start = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const lbm_handle* h = b->h[i];
+    bp.gx[i] = (h->cfg.nx + b->bx - 1) / b->bx;
+    bp.gy[i] = (h->cfg.ny + b->by - 1) / b->by;
+    bp.start[i] = start;
+    start += bp.gx[i] * bp.gy[i] * h->cfg.nz;
+  }
+  bp.start[b->n] = start;
+}
+
+int batch_launch(lbm_batch* b, int kind, const BatchParams& bp, int grid) {
+  b->ops.launch(kind, dim3(grid), dim3(b->bx, b->by), b->stream, bp);
+  b->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "batched launch %d: %s", kind, cudaGetErrorString(e));
+  return 0;
+}
+
+// One forward step of every lattice; results[i] (may be null) gets F of lattice i.
+int batch_forward(lbm_batch* b, double* const* results) {
+  BatchParams bp;
+  batch_layout(b, bp);
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    KParams& p = bp.p[i];
+    p = base_params(h, h->t);
+    p.fin = h->f[h->cur];
+    p.fout = h->f[1 - h->cur];
+    p.eval_obj = (results && results[i] && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+    p.result = results ? results[i] : nullptr;
+  }
+  int rc = batch_launch(b, K_FORWARD, bp, b->grid_fwd);
+  if (rc) return rc;
+  for (int i = 0; i < b->n; ++i) {
+    b->h[i]->cur ^= 1;
+    b->h[i]->t += 1;
+  }
+  return 0;
+}
+
+int batch_objective(lbm_batch* b, double* const* results) {
+  BatchParams bp;
+  batch_layout(b, bp);
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    KParams& p = bp.p[i];
+    p = base_params(h, h->t);
+    p.fin = h->f[h->cur];
+    p.eval_obj = h->cfg.objective != LBM_OBJ_NONE ? 1 : 0;
+    p.result = results[i];
+  }
+  return batch_launch(b, K_OBJECTIVE, bp, b->grid_obj);
+}
+
+int batch_adjoint(lbm_batch* b) {
+  BatchParams bp;
+  batch_layout(b, bp);
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    KParams& p = bp.p[i];
+    p = base_params(h, h->t);
+    p.fin = h->f[h->cur];
+    p.lam_in = h->lam[h->lcur];
+    p.lam_out = h->lam[1 - h->lcur];
+    p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+  }
+  int rc = batch_launch(b, K_ADJOINT, bp, b->grid_adj);
+  if (rc) return rc;
+  for (int i = 0; i < b->n; ++i) b->h[i]->lcur ^= 1;
+  return 0;
+}
+
+// state <-> checkpoint slot of every lattice, one launch
+int batch_copy(lbm_batch* b, int slot, bool to_slot) {
+  CopyBatch cb;
+  cb.n = b->n;
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    void* st = h->f[h->cur];
+    void* sl = h->slots[slot];
+    cb.src[i] = (const uint4*)(to_slot ? st : sl);
+    cb.dst[i] = (uint4*)(to_slot ? sl : st);
+    cb.nvec[i] = (long long)(state_bytes(h) / 16);
+  }
+  k_copy_batch<<<b->grid_copy, 256, 0, b->stream>>>(cb);
+  b->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "batched copy: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int batch_init(lbm_batch* b) {
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    KParams p = base_params(h, 0);
+    p.fout = h->f[h->cur];
+    h->launch(K_INIT, h->geo.grid, h->geo.block, b->stream, p, h->init_mac);
+    b->launches++;
+    h->t = 0;
+    h->have_state = true;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "init: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+// The checkpointed forward + reverse sequence of lbm_batch_gradient, issued on
+// the batch stream (and so capturable as one graph).
+int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
+  int rc;
+  for (int i = 0; i < b->n; ++i) {
+    b->h[i]->cur = 0;
+    b->h[i]->lcur = 0;
+  }
+  WangSchedule ws(nsnap);
+  double* res[LBM_MAX_BATCH];
+  if ((rc = batch_init(b))) return rc;
+  if ((rc = batch_copy(b, ws.make_checkpoint(0), true))) return rc;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev + (s - 1) : nullptr;
+    if ((rc = batch_forward(b, res))) return rc;
+    if ((rc = batch_copy(b, ws.make_checkpoint(s + 1), true))) return rc;
+  }
+  for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev + (nsteps - 1);
+  if ((rc = batch_objective(b, res))) return rc;
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
+    BCUDA(b, cudaMemsetAsync(h->sens, 0, (size_t)h->ncell * sizeof(double), b->stream));
+    h->lcur = 0;
+    h->have_adjoint = true;
+  }
+  WangSchedule::Actions act;
+  act.advance = [&]() { return batch_forward(b, nullptr); };
+  act.restore = [&](int step, int slot) -> int {
+    for (int i = 0; i < b->n; ++i) b->h[i]->t = step;
+    return batch_copy(b, slot, false);
+  };
+  act.save = [&](int slot) { return batch_copy(b, slot, true); };
+  for (int s = nsteps; s >= 1; --s) {
+    try {
+      rc = ws.get_forward_solution(s, act);
+    } catch (const std::exception& ex) {
+      return bfail(b, LBM_ERR_STATE, "checkpoint schedule: %s", ex.what());
+    }
+    if (rc) return rc;
+    if ((rc = batch_adjoint(b))) return rc;
+  }
+  // reverse of the collision of f_0 (see lbm_gradient)
+  if ((rc = batch_init(b))) return rc;
+  if ((rc = batch_adjoint(b))) return rc;
+  *recomputed = ws.recomputed();
+  return 0;
+}
+
+void batch_destroy_graph(lbm_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_steps = b->graph_snap = -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out) {
+  if (!cfgs || !out) return bfail(nullptr, LBM_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (n < 1 || n > LBM_MAX_BATCH) return bfail(nullptr, LBM_ERR_ARG, "batch of %d lattices outside [1,%d]", n, LBM_MAX_BATCH);
+  for (int i = 1; i < n; ++i)
+    if (cfgs[i].lattice != cfgs[0].lattice || cfgs[i].collision != cfgs[0].collision ||
+        cfgs[i].storage != cfgs[0].storage)
+      return bfail(nullptr, LBM_ERR_SUP, "batched lattices must share lattice, collision and storage");
+  lbm_batch* b = new (std::nothrow) lbm_batch();
+  if (!b) return bfail(nullptr, LBM_ERR_MEM, "host allocation failed");
+  for (int i = 0; i < n; ++i) {
+    int rc = lbm_create(&cfgs[i], &b->h[i]);
+    if (rc) {
+      std::string msg = g_create_error;
+      for (int j = 0; j < i; ++j) lbm_destroy(b->h[j]);
+      delete b;
+      return bfail(nullptr, rc, "lattice %d: %s", i, msg.c_str());
+    }
+    b->n = i + 1;
+  }
+  const lbm_config& c = cfgs[0];
+  b->ops = c.lattice == LBM_D2Q9    ? batch_ops_d2q9(c.collision, c.storage)
+           : c.lattice == LBM_D3Q19 ? batch_ops_d3q19(c.collision, c.storage)
+                                    : batch_ops_thermal(c.collision, c.storage);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (b->nsm < 1) b->nsm = 1;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess || !b->ops.launch) {
+    for (int i = 0; i < b->n; ++i) lbm_destroy(b->h[i]);
+    delete b;
+    return bfail(nullptr, LBM_ERR_CUDA, "batch set-up failed");
+  }
+  cudaEventCreate(&b->ev[0]);
+  cudaEventCreate(&b->ev[1]);
+  // default shape: 128x2, one of the autotuner's shapes (partial sums are sized for all)
+  b->bx = 128;
+  b->by = 2;
+  BatchParams bp;
+  batch_layout(b, bp);
+  b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
+  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
+  b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
+  b->grid_copy = 4 * b->nsm;
+  *out = b;
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(lbm_batch* b) {
+  if (!b) return LBM_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_destroy_graph(b);
+  for (int i = 0; i < b->n; ++i) lbm_destroy(b->h[i]);
+  for (cudaEvent_t e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return LBM_OK;
+}
+
+const char* lbm_batch_last_error(const lbm_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+int lbm_batch_handle(lbm_batch* b, int i, lbm_handle** h) {
+  if (!b || !h || i < 0 || i >= b->n) return bfail(b, LBM_ERR_ARG, "lattice index %d", i);
+  *h = b->h[i];
+  return LBM_OK;
+}
+
+int lbm_batch_autotune(lbm_batch* b, int nsteps) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  for (int i = 0; i < b->n; ++i)
+    if (!b->h[i]->have_design) return bfail(b, LBM_ERR_STATE, "lattice %d has no design", i);
+  if (nsteps < 1) nsteps = 3;
+  batch_destroy_graph(b);
+  int rc;
+  if ((rc = batch_init(b))) return rc;
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
+    h->have_adjoint = true;
+    h->t = 1;
+  }
+  float best = 1e30f;
+  int bbx = b->bx, bby = b->by;
+  for (const auto& sh : kShapes) {
+    b->bx = sh[0];
+    b->by = sh[1];
+    BatchParams bp;
+    batch_layout(b, bp);
+    b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
+    b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
+    if ((rc = batch_forward(b, nullptr)) || (rc = batch_adjoint(b))) return rc;
+    cudaEventRecord(b->ev[0], b->stream);
+    for (int k = 0; k < nsteps && !rc; ++k) {
+      rc = batch_forward(b, nullptr);
+      if (!rc) rc = batch_adjoint(b);
+    }
+    cudaEventRecord(b->ev[1], b->stream);
+    if (rc) return rc;
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+    if (ms < best) {
+      best = ms;
+      bbx = sh[0];
+      bby = sh[1];
+    }
+  }
+  b->bx = bbx;
+  b->by = bby;
+  BatchParams bp;
+  batch_layout(b, bp);
+  b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
+  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
+  b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
+  if ((rc = batch_init(b))) return rc;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by) {
+  if (!b || !bx || !by) return bfail(nullptr, LBM_ERR_ARG, "null argument");
+  *bx = b->bx;
+  *by = b->by;
+  return LBM_OK;
+}
+
+int lbm_batch_forward(lbm_batch* b, int nsteps, double* J) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  if (nsteps < 1) return bfail(b, LBM_ERR_ARG, "nsteps %d < 1", nsteps);
+  for (int i = 0; i < b->n; ++i) {
+    if (!b->h[i]->have_design || !b->h[i]->have_state)
+      return bfail(b, LBM_ERR_STATE, "lattice %d has no design or state", i);
+    if (ensure_jcap(b->h[i], (size_t)nsteps)) return bfail(b, LBM_ERR_MEM, "%s", b->h[i]->err.c_str());
+  }
+  int rc;
+  double* res[LBM_MAX_BATCH];
+  for (int s = 0; s < nsteps; ++s) {
+    for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev + (s - 1) : nullptr;
+    if ((rc = batch_forward(b, res))) return rc;
+  }
+  for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev + (nsteps - 1);
+  if ((rc = batch_objective(b, res))) return rc;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (J) {
+    std::vector<double> js((size_t)nsteps);
+    for (int i = 0; i < b->n; ++i) {
+      BCUDA(b, cudaMemcpy(js.data(), b->h[i]->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      double acc = 0.;
+      for (double v : js) acc += v;
+      J[i] = acc;
+    }
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, double* J,
+                       double* const* dJdgamma, lbm_gradient_stats* stats) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  if (nsteps < 1 || nsnap < 2) return bfail(b, LBM_ERR_ARG, "need nsteps >= 1 and nsnapshots >= 2");
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    if (!h->have_design) return bfail(b, LBM_ERR_STATE, "lattice %d has no design", i);
+    if (ensure_jcap(h, (size_t)nsteps)) return bfail(b, LBM_ERR_MEM, "%s", h->err.c_str());
+    if ((int)h->slots.size() != nsnap) {
+      batch_destroy_graph(b);
+      for (void* s : h->slots)
+        if (s) cudaFree(s);
+      h->slots.assign(nsnap, nullptr);
+      for (int k = 0; k < nsnap; ++k) {
+        if (cudaMalloc(&h->slots[k], state_bytes(h)) != cudaSuccess) {
+          for (void* s : h->slots)
+            if (s) cudaFree(s);
+          h->slots.clear();
+          return bfail(b, LBM_ERR_MEM, "lattice %d: %d snapshot slots", i, nsnap);
+        }
+      }
+    }
+  }
+  int rc;
+  int64_t recomputed = 0;
+  cudaEventRecord(b->ev[0], b->stream);
+  if (use_graph) {
+    if (!(b->graph && b->graph_steps == nsteps && b->graph_snap == nsnap)) {
+      batch_destroy_graph(b);
+      cudaGraph_t g = nullptr;
+      const int64_t l0 = b->launches;
+      BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      rc = batch_sequence(b, nsteps, nsnap, &recomputed);
+      b->graph_launches = b->launches - l0;
+      cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        b->graph = nullptr;
+        return bfail(b, LBM_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+      }
+      b->graph_steps = nsteps;
+      b->graph_snap = nsnap;
+      b->graph_recomputed = recomputed;
+      for (int i = 0; i < b->n; ++i) {
+        b->end_cur[i] = b->h[i]->cur;
+        b->end_lcur[i] = b->h[i]->lcur;
+      }
+      b->launches -= b->graph_launches;   // counted again below, per replay
+      cudaEventRecord(b->ev[0], b->stream);
+    } else {
+      recomputed = b->graph_recomputed;
+    }
+    BCUDA(b, cudaGraphLaunch(b->graph, b->stream));
+    b->launches += b->graph_launches;
+    // the replayed sequence starts from f_0 in buffer 0 whatever the handles held
+    // before, and leaves them as the captured sequence did
+    for (int i = 0; i < b->n; ++i) {
+      lbm_handle* h = b->h[i];
+      h->cur = b->end_cur[i];
+      h->lcur = b->end_lcur[i];
+      h->t = 0;
+      h->have_state = h->have_adjoint = true;
+    }
+  } else {
+    if ((rc = batch_sequence(b, nsteps, nsnap, &recomputed))) return rc;
+  }
+  cudaEventRecord(b->ev[1], b->stream);
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+  std::vector<double> js((size_t)nsteps);
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    if (J) {
+      BCUDA(b, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      double acc = 0.;
+      for (double v : js) acc += v;
+      if (!std::isfinite(acc)) return bfail(b, LBM_ERR_NONFINITE, "lattice %d: objective not finite", i);
+      J[i] = acc;
+    }
+    if (dJdgamma && dJdgamma[i])
+      BCUDA(b, cudaMemcpy(dJdgamma[i], h->sens, (size_t)h->ncell * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (stats) {
+    stats->forward_steps = nsteps;
+    stats->recomputed_steps = recomputed;
+    stats->adjoint_steps = nsteps;
+    stats->forward_ms = ms;   // whole sequence (one graph launch when use_graph)
+    stats->reverse_ms = 0.;
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_time_steps(lbm_batch* b, int which, int nsteps, float* ms) {
+  if (!b || !ms || nsteps < 1 || which < 0 || which > 2) return bfail(b, LBM_ERR_ARG, "bad arguments");
+  for (int i = 0; i < b->n; ++i)
+    if (!b->h[i]->have_design || !b->h[i]->have_state)
+      return bfail(b, LBM_ERR_STATE, "lattice %d has no design or state", i);
+  int rc;
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    if (which >= 1 && !h->have_adjoint) {
+      for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
+      h->have_adjoint = true;
+    }
+    if (which >= 1 && h->t < 1) h->t = 1;
+  }
+  cudaEventRecord(b->ev[0], b->stream);
+  for (int k = 0; k < nsteps; ++k) {
+    if (which != 1 && (rc = batch_forward(b, nullptr))) return rc;
+    if (which != 0 && (rc = batch_adjoint(b))) return rc;
+  }
+  cudaEventRecord(b->ev[1], b->stream);
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  cudaEventElapsedTime(ms, b->ev[0], b->ev[1]);
+  return LBM_OK;
+}
+
+int lbm_batch_get_launch_count(const lbm_batch* b, int64_t* n) {
+  if (!b || !n) return bfail(nullptr, LBM_ERR_ARG, "null argument");
+  *n = b->launches;
+  return LBM_OK;
+}
+
+}  // extern "C"

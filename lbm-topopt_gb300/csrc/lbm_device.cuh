@@ -1325,14 +1325,14 @@ __device__ __forceinline__ C warp_sum(C v) {
   return v;
 }
 
+// bid / nblk: this block's index and the block count of its lattice.
 template <class C>
-__device__ __forceinline__ void grid_reduce(C v, const KParams& p) {
+__device__ __forceinline__ void grid_reduce_v(C v, const KParams& p, unsigned bid, unsigned nblk) {
   __shared__ double sh[32];
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nthr = blockDim.x * blockDim.y;
-  const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
-  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  __syncthreads();   // the shared slots may still be read from a previous call
   // warps whose cells contribute nothing (e.g. away from the pressure-drop
   // strips) skip the shuffle tree
   if (__any_sync(0xffffffffu, v != C(0.))) v = warp_sum(v);
@@ -1362,5 +1362,24 @@ __device__ __forceinline__ void grid_reduce(C v, const KParams& p) {
     *p.counter = 0u;
   }
 }
+
+template <class C>
+__device__ __forceinline__ void grid_reduce(C v, const KParams& p) {
+  const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  grid_reduce_v(v, p, bid, nblk);
+}
+
+// ---------------------------------------------------------------------------
+// Launch parameters of a batch of lattices advanced by one launch.
+
+constexpr int kMaxBatch = LBM_MAX_BATCH;
+
+struct BatchParams {
+  int n;                        // lattices in the batch
+  int start[kMaxBatch + 1];     // first virtual block of each lattice; start[n] = total
+  int gx[kMaxBatch], gy[kMaxBatch];   // blocks along x and y of each lattice (z: one per plane)
+  KParams p[kMaxBatch];
+};
 
 }  // namespace lbm

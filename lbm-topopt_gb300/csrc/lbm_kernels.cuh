@@ -152,15 +152,15 @@ __device__ __forceinline__ void pull_all(C* lam, const A* __restrict__ lin, int 
 
 // ---------------------------------------------------------------------------
 
+// Per-cell bodies, shared by the single-lattice kernels and the batched ones.
+
+// Forward step of cell (x,y,z); returns its objective contribution F(f_t).
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
+__device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, int x, int y, int z) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
   constexpr bool SHIFT = Store<S>::SHIFT;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
   C objv = C(0.);
   if (x < p.nx && y < p.ny) {
     const int c = (z * p.ny + y) * p.nx + x;
@@ -180,19 +180,17 @@ __global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
     }
     push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
   }
-  if (p.eval_obj) grid_reduce(objv, p);
+  return objv;
 }
 
+// Reverse step of cell (x,y,z).
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::adj) k_adjoint(KParams p) {
+__device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int z) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
   using A = typename AdjT<S>::T;
   constexpr bool SHIFT = Store<S>::SHIFT;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
   if (x >= p.nx || y >= p.ny) return;
   const int c = (z * p.ny + y) * p.nx + x;
   const A* __restrict__ lin = (const A*)p.lam_in;
@@ -228,16 +226,14 @@ __global__ void __launch_bounds__(256, Occupancy<S>::adj) k_adjoint(KParams p) {
   p.sens[c] += (double)dg;
 }
 
-// Objective of the state f_t alone (the last step of a forward sweep).
+// Objective of the state f_t at cell (x,y,z) alone.
 template <int LAT, class S>
-__global__ void __launch_bounds__(256) k_objective(KParams p) {
+__device__ __forceinline__ typename Store<S>::C objective_only_cell(const KParams& p, int x, int y,
+                                                                   int z) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
   constexpr bool SHIFT = Store<S>::SHIFT;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
   C v = C(0.);
   if (x < p.nx && y < p.ny) {
     const int c = (z * p.ny + y) * p.nx + x;
@@ -246,7 +242,83 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
     if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     v = objective_cell<LAT, SHIFT>(f, C(((const G*)p.gamma)[c]), x, y, z, p);
   }
-  grid_reduce(v, p);
+  return v;
+}
+
+template <int LAT, int COLL, class S>
+__global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const auto objv = forward_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
+  if (p.eval_obj) grid_reduce(objv, p);
+}
+
+template <int LAT, int COLL, class S>
+__global__ void __launch_bounds__(256, Occupancy<S>::adj) k_adjoint(KParams p) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  adjoint_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
+}
+
+// Objective of the state f_t alone (the last step of a forward sweep).
+template <int LAT, class S>
+__global__ void __launch_bounds__(256) k_objective(KParams p) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  grid_reduce(objective_only_cell<LAT, S>(p, x, y, blockIdx.z), p);
+}
+
+// ---------------------------------------------------------------------------
+// Batched kernels: one launch advances every lattice of a batch (uneven sizes,
+// each with its own boundaries, design and objective).  The virtual blocks of
+// all lattices are concatenated; a persistent grid of resident blocks strides
+// over them, so small and large lattices share the SMs.  Per-lattice
+// parameters are read in place from the launch's parameter space.
+
+template <int LAT, int COLL, class S>
+__global__ void __launch_bounds__(256, Occupancy<S>::fwd)
+    k_forward_batch(const __grid_constant__ BatchParams bp) {
+  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
+    int i = 0;
+    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+    const KParams& p = bp.p[i];
+    const int lb = vb - bp.start[i];
+    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
+    const auto objv = forward_cell<LAT, COLL, S>(p, x, y, r / bp.gy[i]);
+    if (p.eval_obj) grid_reduce_v(objv, p, lb, bp.start[i + 1] - bp.start[i]);
+  }
+}
+
+template <int LAT, int COLL, class S>
+__global__ void __launch_bounds__(256, Occupancy<S>::adj)
+    k_adjoint_batch(const __grid_constant__ BatchParams bp) {
+  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
+    int i = 0;
+    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+    const KParams& p = bp.p[i];
+    const int lb = vb - bp.start[i];
+    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
+    adjoint_cell<LAT, COLL, S>(p, x, y, r / bp.gy[i]);
+  }
+}
+
+template <int LAT, class S>
+__global__ void __launch_bounds__(256) k_objective_batch(const __grid_constant__ BatchParams bp) {
+  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
+    int i = 0;
+    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+    const KParams& p = bp.p[i];
+    const int lb = vb - bp.start[i];
+    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
+    const int x = bx * blockDim.x + threadIdx.x;
+    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
+    const auto v = objective_only_cell<LAT, S>(p, x, y, r / bp.gy[i]);
+    if (p.eval_obj) grid_reduce_v(v, p, lb, bp.start[i + 1] - bp.start[i]);
+  }
 }
 
 // f~_0 = feq(macros) (IsoEquilibriumInitializationLoop2d, isothermalLBLoops2d.hh:264-285;
@@ -375,6 +447,33 @@ __global__ void k_gamma(const double* __restrict__ src, G* __restrict__ dst, lon
 
 template <int LAT, int COLL, class S>
 struct OpsImpl {
+  static void launch_batch(int kind, dim3 grid, dim3 block, cudaStream_t st, const BatchParams& bp) {
+    switch (kind) {
+      case K_FORWARD:
+        k_forward_batch<LAT, COLL, S><<<grid, block, 0, st>>>(bp);
+        break;
+      case K_ADJOINT:
+        k_adjoint_batch<LAT, COLL, S><<<grid, block, 0, st>>>(bp);
+        break;
+      case K_OBJECTIVE:
+        k_objective_batch<LAT, S><<<grid, block, 0, st>>>(bp);
+        break;
+      default:
+        break;
+    }
+  }
+  static const void* kernel_address(int kind) {
+    switch (kind) {
+      case K_FORWARD:
+        return (const void*)k_forward_batch<LAT, COLL, S>;
+      case K_ADJOINT:
+        return (const void*)k_adjoint_batch<LAT, COLL, S>;
+      case K_OBJECTIVE:
+        return (const void*)k_objective_batch<LAT, S>;
+      default:
+        return nullptr;
+    }
+  }
   static void launch(int kind, dim3 grid, dim3 block, cudaStream_t st, const KParams& p,
                      double* aux) {
     switch (kind) {

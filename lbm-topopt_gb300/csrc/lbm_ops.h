@@ -8,6 +8,7 @@
 namespace lbm {
 
 struct KParams;
+struct BatchParams;
 
 enum {
   K_FORWARD = 0,
@@ -23,6 +24,19 @@ enum {
 
 typedef void (*LaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st, const KParams& p,
                          double* aux);
+
+typedef void (*BatchLaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st,
+                              const BatchParams& bp);
+typedef const void* (*KernelAddressFn)(int kind);
+
+struct BatchOps {
+  BatchLaunchFn launch = nullptr;
+  KernelAddressFn kernel = nullptr;
+};
+
+BatchOps batch_ops_d2q9(int collision, int storage);
+BatchOps batch_ops_d3q19(int collision, int storage);
+BatchOps batch_ops_thermal(int collision, int storage);
 
 LaunchFn launcher_d2q9(int collision, int storage);
 LaunchFn launcher_d3q19(int collision, int storage);

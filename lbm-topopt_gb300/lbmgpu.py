@@ -194,6 +194,17 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_time_steps": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
         "lbm_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
         "lbm_select_device": (C.c_int, [C.c_int]),
+        "lbm_batch_create": (C.c_int, [C.POINTER(CConfig), C.c_int, C.POINTER(H)]),
+        "lbm_batch_destroy": (C.c_int, [H]),
+        "lbm_batch_last_error": (C.c_char_p, [H]),
+        "lbm_batch_handle": (C.c_int, [H, C.c_int, C.POINTER(H)]),
+        "lbm_batch_autotune": (C.c_int, [H, C.c_int]),
+        "lbm_batch_get_launch_shape": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_batch_forward": (C.c_int, [H, C.c_int, dp]),
+        "lbm_batch_gradient": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp, C.POINTER(dp),
+                                         C.POINTER(CGradStats)]),
+        "lbm_batch_time_steps": (C.c_int, [H, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+        "lbm_batch_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
         "lbm_autotune": (C.c_int, [H, C.c_int]),
         "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
@@ -345,6 +356,95 @@ class Handle:
     def launch_count(self) -> int:
         n = C.c_int64()
         self._check(self.lib.lbm_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+
+class _View(Handle):
+    """A lattice owned by a Batch (not destroyed on its own)."""
+
+    def __init__(self, lib, cfg, h):  # noqa: D401 - plain holder
+        self.lib, self.cfg, self.h = lib, cfg, h
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Several lattices advanced by one launch per time step (lbm_batch_*)."""
+
+    def __init__(self, cfgs: Sequence[Config]):
+        self.lib = load_library()
+        self.cfgs = list(cfgs)
+        arr = (CConfig * len(self.cfgs))(*[c.to_c() for c in self.cfgs])
+        self._arr = arr
+        b = C.c_void_p()
+        rc = self.lib.lbm_batch_create(arr, len(self.cfgs), C.byref(b))
+        if rc:
+            raise LBMError(rc, self.lib.lbm_batch_last_error(None).decode())
+        self.b = b
+        self.views = []
+        for i, cfg in enumerate(self.cfgs):
+            h = C.c_void_p()
+            self._check(self.lib.lbm_batch_handle(self.b, i, C.byref(h)))
+            self.views.append(_View(self.lib, cfg, h))
+
+    def _check(self, rc):
+        if rc:
+            raise LBMError(rc, self.lib.lbm_batch_last_error(self.b).decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            for v in self.views:
+                v.h = None
+            self.lib.lbm_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __getitem__(self, i) -> Handle:
+        return self.views[i]
+
+    def __len__(self):
+        return len(self.views)
+
+    def autotune(self, nsteps: int = 3):
+        self._check(self.lib.lbm_batch_autotune(self.b, int(nsteps)))
+        bx, by = C.c_int(), C.c_int()
+        self._check(self.lib.lbm_batch_get_launch_shape(self.b, C.byref(bx), C.byref(by)))
+        return bx.value, by.value
+
+    def forward(self, nsteps: int):
+        J = np.zeros(len(self))
+        self._check(self.lib.lbm_batch_forward(self.b, int(nsteps), _ptr(J)))
+        return J
+
+    def gradient(self, nsteps: int, nsnapshots: int, use_graph: bool = True):
+        J = np.zeros(len(self))
+        sens = [np.empty(c.ncells) for c in self.cfgs]
+        ptrs = (C.POINTER(C.c_double) * len(self))(*[_ptr(a) for a in sens])
+        st = CGradStats()
+        self._check(self.lib.lbm_batch_gradient(self.b, int(nsteps), int(nsnapshots),
+                                                int(bool(use_graph)), _ptr(J), ptrs, C.byref(st)))
+        return J, sens, st
+
+    def time_steps(self, which: int, nsteps: int) -> float:
+        ms = C.c_float()
+        self._check(self.lib.lbm_batch_time_steps(self.b, int(which), int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.lbm_batch_get_launch_count(self.b, C.byref(n)))
         return n.value
 
 
