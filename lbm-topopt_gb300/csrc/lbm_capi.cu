@@ -17,6 +17,7 @@
 #include "../../include/lbmgpu.h"
 #include "lbm_device.cuh"
 #include "lbm_ops.h"
+#include "state_pool.hpp"
 #include "wang.hpp"
 
 using namespace lbm;
@@ -328,32 +329,44 @@ int ensure_stage(lbm_handle* h) {
   return 0;
 }
 
-// One forward step f~_t -> f~_{t+1}; result (may be null) receives F(f_t).
-int forward_step(lbm_handle* h, double* result) {
+// Buffer b of a handle's state pool: 0 and 1 are the state buffers, 2 .. K+1
+// the checkpoint slots' (see StatePool).
+void* pool_buffer(lbm_handle* h, int b) { return b < 2 ? h->f[b] : h->slots[b - 2]; }
+
+// One forward step f~_t (in) -> f~_{t+1} (out); result (may be null) receives F(f_t).
+int forward_launch(lbm_handle* h, const void* in, void* out, double* result) {
   KParams p = base_params(h, h->t);
-  p.fin = h->f[h->cur];
-  p.fout = h->f[1 - h->cur];
+  p.fin = in;
+  p.fout = out;
   p.eval_obj = (result != nullptr && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
   p.result = result;
   int rc = launch(h, K_FORWARD, p, nullptr);
   if (rc) return rc;
-  h->cur ^= 1;
   h->t += 1;
   return 0;
 }
 
-int objective_only(lbm_handle* h, double* result) {
+int forward_step(lbm_handle* h, double* result) {
+  int rc = forward_launch(h, h->f[h->cur], h->f[1 - h->cur], result);
+  if (rc) return rc;
+  h->cur ^= 1;
+  return 0;
+}
+
+int objective_at(lbm_handle* h, const void* f, double* result) {
   KParams p = base_params(h, h->t);
-  p.fin = h->f[h->cur];
+  p.fin = f;
   p.eval_obj = 1;
   p.result = result;
   return launch(h, K_OBJECTIVE, p, nullptr);
 }
 
-// One reverse step at the current forward state f_t.
-int adjoint_step(lbm_handle* h) {
+int objective_only(lbm_handle* h, double* result) { return objective_at(h, h->f[h->cur], result); }
+
+// One reverse step at the forward state f_t held in `f`.
+int adjoint_at(lbm_handle* h, const void* f) {
   KParams p = base_params(h, h->t);
-  p.fin = h->f[h->cur];
+  p.fin = f;
   p.lam_in = h->lam[h->lcur];
   p.lam_out = h->lam[1 - h->lcur];
   p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
@@ -362,6 +375,8 @@ int adjoint_step(lbm_handle* h) {
   h->lcur ^= 1;
   return 0;
 }
+
+int adjoint_step(lbm_handle* h) { return adjoint_at(h, h->f[h->cur]); }
 
 int sync(lbm_handle* h) {
   cudaError_t e = cudaStreamSynchronize(h->stream);
@@ -376,15 +391,17 @@ int zero_adjoint(lbm_handle* h) {
   return 0;
 }
 
-int init_state(lbm_handle* h) {
+int init_into(lbm_handle* h, void* out) {
   KParams p = base_params(h, 0);
-  p.fout = h->f[h->cur];
+  p.fout = out;
   int rc = launch(h, K_INIT, p, h->init_mac);
   if (rc) return rc;
   h->t = 0;
   h->have_state = true;
   return 0;
 }
+
+int init_state(lbm_handle* h) { return init_into(h, h->f[h->cur]); }
 
 }  // namespace
 
@@ -746,27 +763,45 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
   const bool obj = h->cfg.objective != LBM_OBJ_NONE;
   const size_t sb = state_bytes(h);
   WangSchedule ws(nsnap);
+  // Checkpoints without copies: every state lives in one of the pool's K+2
+  // buffers and saves/restores only move labels (StatePool).
+  StatePool pool;
+  pool.reset(nsnap, h->cur);
+  auto cur_buf = [&]() { return pool_buffer(h, pool.current()); };
+  auto advance = [&](double* result) -> int {
+    const int out = pool.scratch();
+    int r = forward_launch(h, cur_buf(), pool_buffer(h, out), result);
+    if (!r) pool.set_current(out);
+    return r;
+  };
   auto save = [&](int slot) -> int {
-    CUDA_OR_FAIL(h, cudaMemcpyAsync(h->slots[slot], h->f[h->cur], sb, cudaMemcpyDeviceToDevice, h->stream));
+    const int dst = pool.save(slot);
+    if (dst >= 0)
+      CUDA_OR_FAIL(h, cudaMemcpyAsync(pool_buffer(h, dst), cur_buf(), sb, cudaMemcpyDeviceToDevice,
+                                      h->stream));
     return 0;
   };
   WangSchedule::Actions act;
-  act.advance = [&]() { return forward_step(h, nullptr); };
+  act.advance = [&]() { return advance(nullptr); };
   act.restore = [&](int step, int slot) -> int {
-    CUDA_OR_FAIL(h, cudaMemcpyAsync(h->f[h->cur], h->slots[slot], sb, cudaMemcpyDeviceToDevice, h->stream));
+    pool.restore(slot);
     h->t = step;
     return 0;
   };
   act.save = save;
 
   cudaEventRecord(h->ev[0], h->stream);
-  if ((rc = init_state(h))) return rc;
+  {
+    const int out = pool.scratch();
+    if ((rc = init_into(h, pool_buffer(h, out)))) return rc;
+    pool.set_current(out);
+  }
   if ((rc = save(ws.make_checkpoint(0)))) return rc;
   for (int s = 0; s < nsteps; ++s) {
-    if ((rc = forward_step(h, (obj && s >= 1) ? h->jdev + (s - 1) : nullptr))) return rc;
+    if ((rc = advance((obj && s >= 1) ? h->jdev + (s - 1) : nullptr))) return rc;
     if ((rc = save(ws.make_checkpoint(s + 1)))) return rc;
   }
-  if (obj && (rc = objective_only(h, h->jdev + (nsteps - 1)))) return rc;
+  if (obj && (rc = objective_at(h, cur_buf(), h->jdev + (nsteps - 1)))) return rc;
   cudaEventRecord(h->ev[1], h->stream);
   if ((rc = zero_adjoint(h))) return rc;
   h->have_adjoint = true;
@@ -777,11 +812,13 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
       return fail(h, LBM_ERR_STATE, "checkpoint schedule: %s", ex.what());
     }
     if (rc) return rc;
-    if ((rc = adjoint_step(h))) return rc;
+    if ((rc = adjoint_at(h, cur_buf()))) return rc;
   }
   // The collision of f_0 depends on the design too; the reference's reverse loop stops
   // at step 1 (robustPump2d.cc:268-276).  Reverse it as well: no objective and no
   // boundary at t = 0.  The term is exactly zero for isothermal flows started at rest.
+  // Every checkpoint has been consumed, so f_0 goes back into state buffer 0.
+  h->cur = 0;
   if ((rc = init_state(h))) return rc;
   if ((rc = adjoint_step(h))) return rc;
   cudaEventRecord(h->ev[2], h->stream);
@@ -1037,50 +1074,64 @@ int batch_launch(lbm_batch* b, int kind, const BatchParams& bp, int grid) {
   return 0;
 }
 
-// One forward step of every lattice; results[i] (may be null) gets F of lattice i.
-int batch_forward(lbm_batch* b, double* const* results) {
+// Buffers are named by StatePool index, or per lattice as its current state
+// buffer / its other state buffer.
+constexpr int kCurState = -1, kOtherState = -2;
+
+void* batch_buffer(lbm_handle* h, int b) {
+  return b == kCurState ? h->f[h->cur] : b == kOtherState ? h->f[1 - h->cur] : pool_buffer(h, b);
+}
+
+// One forward step of every lattice from buffer `in` into buffer `out`;
+// results[i] (may be null) gets F of lattice i.
+int batch_forward_bufs(lbm_batch* b, int in, int out, double* const* results) {
   BatchParams bp;
   batch_layout(b, bp);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
     p = base_params(h, h->t);
-    p.fin = h->f[h->cur];
-    p.fout = h->f[1 - h->cur];
+    p.fin = batch_buffer(h, in);
+    p.fout = batch_buffer(h, out);
     p.eval_obj = (results && results[i] && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
     p.result = results ? results[i] : nullptr;
   }
   int rc = batch_launch(b, K_FORWARD, bp, b->grid_fwd);
   if (rc) return rc;
-  for (int i = 0; i < b->n; ++i) {
-    b->h[i]->cur ^= 1;
-    b->h[i]->t += 1;
-  }
+  for (int i = 0; i < b->n; ++i) b->h[i]->t += 1;
   return 0;
 }
 
-int batch_objective(lbm_batch* b, double* const* results) {
+// One forward step of every lattice between its two state buffers.
+int batch_forward(lbm_batch* b, double* const* results) {
+  int rc = batch_forward_bufs(b, kCurState, kOtherState, results);
+  if (rc) return rc;
+  for (int i = 0; i < b->n; ++i) b->h[i]->cur ^= 1;
+  return 0;
+}
+
+int batch_objective(lbm_batch* b, int buf, double* const* results) {
   BatchParams bp;
   batch_layout(b, bp);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
     p = base_params(h, h->t);
-    p.fin = h->f[h->cur];
+    p.fin = batch_buffer(h, buf);
     p.eval_obj = h->cfg.objective != LBM_OBJ_NONE ? 1 : 0;
     p.result = results[i];
   }
   return batch_launch(b, K_OBJECTIVE, bp, b->grid_obj);
 }
 
-int batch_adjoint(lbm_batch* b) {
+int batch_adjoint(lbm_batch* b, int buf) {
   BatchParams bp;
   batch_layout(b, bp);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
     p = base_params(h, h->t);
-    p.fin = h->f[h->cur];
+    p.fin = batch_buffer(h, buf);
     p.lam_in = h->lam[h->lcur];
     p.lam_out = h->lam[1 - h->lcur];
     p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
@@ -1091,16 +1142,14 @@ int batch_adjoint(lbm_batch* b) {
   return 0;
 }
 
-// state <-> checkpoint slot of every lattice, one launch
-int batch_copy(lbm_batch* b, int slot, bool to_slot) {
+// dst <- src for every lattice (pool-buffer indices), one launch
+int batch_copy(lbm_batch* b, int src, int dst) {
   CopyBatch cb;
   cb.n = b->n;
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
-    void* st = h->f[h->cur];
-    void* sl = h->slots[slot];
-    cb.src[i] = (const uint4*)(to_slot ? st : sl);
-    cb.dst[i] = (uint4*)(to_slot ? sl : st);
+    cb.src[i] = (const uint4*)batch_buffer(h, src);
+    cb.dst[i] = (uint4*)batch_buffer(h, dst);
     cb.nvec[i] = (long long)(state_bytes(h) / 16);
   }
   k_copy_batch<<<b->grid_copy, 256, 0, b->stream>>>(cb);
@@ -1110,11 +1159,11 @@ int batch_copy(lbm_batch* b, int slot, bool to_slot) {
   return 0;
 }
 
-int batch_init(lbm_batch* b) {
+int batch_init(lbm_batch* b, int buf) {
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams p = base_params(h, 0);
-    p.fout = h->f[h->cur];
+    p.fout = batch_buffer(h, buf);
     h->launch(K_INIT, h->geo.grid, h->geo.block, b->stream, p, h->init_mac);
     b->launches++;
     h->t = 0;
@@ -1126,7 +1175,8 @@ int batch_init(lbm_batch* b) {
 }
 
 // The checkpointed forward + reverse sequence of lbm_batch_gradient, issued on
-// the batch stream (and so capturable as one graph).
+// the batch stream (and so capturable as one graph).  All lattices follow one
+// schedule, so one StatePool labels the buffers of every lattice alike.
 int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
   int rc;
   for (int i = 0; i < b->n; ++i) {
@@ -1134,16 +1184,32 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
     b->h[i]->lcur = 0;
   }
   WangSchedule ws(nsnap);
+  StatePool pool;
+  pool.reset(nsnap, 0);
   double* res[LBM_MAX_BATCH];
-  if ((rc = batch_init(b))) return rc;
-  if ((rc = batch_copy(b, ws.make_checkpoint(0), true))) return rc;
+  auto advance = [&](double* const* results) -> int {
+    const int out = pool.scratch();
+    int r = batch_forward_bufs(b, pool.current(), out, results);
+    if (!r) pool.set_current(out);
+    return r;
+  };
+  auto save = [&](int slot) -> int {
+    const int dst = pool.save(slot);
+    return dst >= 0 ? batch_copy(b, pool.current(), dst) : 0;
+  };
+  {
+    const int out = pool.scratch();
+    if ((rc = batch_init(b, out))) return rc;
+    pool.set_current(out);
+  }
+  if ((rc = save(ws.make_checkpoint(0)))) return rc;
   for (int s = 0; s < nsteps; ++s) {
     for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev + (s - 1) : nullptr;
-    if ((rc = batch_forward(b, res))) return rc;
-    if ((rc = batch_copy(b, ws.make_checkpoint(s + 1), true))) return rc;
+    if ((rc = advance(res))) return rc;
+    if ((rc = save(ws.make_checkpoint(s + 1)))) return rc;
   }
   for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev + (nsteps - 1);
-  if ((rc = batch_objective(b, res))) return rc;
+  if ((rc = batch_objective(b, pool.current(), res))) return rc;
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
@@ -1152,12 +1218,13 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
     h->have_adjoint = true;
   }
   WangSchedule::Actions act;
-  act.advance = [&]() { return batch_forward(b, nullptr); };
+  act.advance = [&]() { return advance(nullptr); };
   act.restore = [&](int step, int slot) -> int {
     for (int i = 0; i < b->n; ++i) b->h[i]->t = step;
-    return batch_copy(b, slot, false);
+    pool.restore(slot);
+    return 0;
   };
-  act.save = [&](int slot) { return batch_copy(b, slot, true); };
+  act.save = save;
   for (int s = nsteps; s >= 1; --s) {
     try {
       rc = ws.get_forward_solution(s, act);
@@ -1165,11 +1232,11 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
       return bfail(b, LBM_ERR_STATE, "checkpoint schedule: %s", ex.what());
     }
     if (rc) return rc;
-    if ((rc = batch_adjoint(b))) return rc;
+    if ((rc = batch_adjoint(b, pool.current()))) return rc;
   }
-  // reverse of the collision of f_0 (see lbm_gradient)
-  if ((rc = batch_init(b))) return rc;
-  if ((rc = batch_adjoint(b))) return rc;
+  // reverse of the collision of f_0 (see lbm_gradient), from state buffer 0
+  if ((rc = batch_init(b, 0))) return rc;
+  if ((rc = batch_adjoint(b, 0))) return rc;
   *recomputed = ws.recomputed();
   return 0;
 }
@@ -1259,7 +1326,7 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
   if (nsteps < 1) nsteps = 3;
   batch_destroy_graph(b);
   int rc;
-  if ((rc = batch_init(b))) return rc;
+  if ((rc = batch_init(b, kCurState))) return rc;
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
@@ -1275,11 +1342,11 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
     batch_layout(b, bp);
     b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
     b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
-    if ((rc = batch_forward(b, nullptr)) || (rc = batch_adjoint(b))) return rc;
+    if ((rc = batch_forward(b, nullptr)) || (rc = batch_adjoint(b, kCurState))) return rc;
     cudaEventRecord(b->ev[0], b->stream);
     for (int k = 0; k < nsteps && !rc; ++k) {
       rc = batch_forward(b, nullptr);
-      if (!rc) rc = batch_adjoint(b);
+      if (!rc) rc = batch_adjoint(b, kCurState);
     }
     cudaEventRecord(b->ev[1], b->stream);
     if (rc) return rc;
@@ -1299,7 +1366,7 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
   b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
   b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
   b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
-  if ((rc = batch_init(b))) return rc;
+  if ((rc = batch_init(b, kCurState))) return rc;
   BCUDA(b, cudaStreamSynchronize(b->stream));
   return LBM_OK;
 }
@@ -1326,7 +1393,7 @@ int lbm_batch_forward(lbm_batch* b, int nsteps, double* J) {
     if ((rc = batch_forward(b, res))) return rc;
   }
   for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev + (nsteps - 1);
-  if ((rc = batch_objective(b, res))) return rc;
+  if ((rc = batch_objective(b, kCurState, res))) return rc;
   BCUDA(b, cudaStreamSynchronize(b->stream));
   if (J) {
     std::vector<double> js((size_t)nsteps);
@@ -1456,7 +1523,7 @@ int lbm_batch_time_steps(lbm_batch* b, int which, int nsteps, float* ms) {
   cudaEventRecord(b->ev[0], b->stream);
   for (int k = 0; k < nsteps; ++k) {
     if (which != 1 && (rc = batch_forward(b, nullptr))) return rc;
-    if (which != 0 && (rc = batch_adjoint(b))) return rc;
+    if (which != 0 && (rc = batch_adjoint(b, kCurState))) return rc;
   }
   cudaEventRecord(b->ev[1], b->stream);
   BCUDA(b, cudaStreamSynchronize(b->stream));

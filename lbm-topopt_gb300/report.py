@@ -1,0 +1,208 @@
+"""Measurements of the five workloads on the GPU, one JSON line each.
+
+    python lbm-topopt_gb300/report.py [--configs 1 2 3 4 5] [--quick]
+
+1  128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps: forward and gradient time,
+   agreement with the FP64 oracle.
+2  1024x512 D2Q9, unsteady inlet, dissipated energy, 20000 steps with 64
+   device snapshots: gradient wall time FP64 vs FP32 shifted storage, FP32
+   error against FP64, dJ/dgamma against central differences (h = 1e-6, FP64)
+   at 16 seeded cells on a 2000-step horizon (one inlet period), and against
+   the reference adjoint (the oracle, bit-identical to the reference's own
+   operators) on a 128x64 cut-down.
+3  256x128x128 D3Q19 MRT duct: FP64 / FP32 / FP16 storage MLUPS and errors
+   (bench.py measures its FP32 headline).
+4  512x256 D2Q9 + D2Q5 thermal, 10000 steps, FP32 with FP64 objective
+   accumulation: gradient time, error against FP64.
+5  8 D2Q9 lattices (3 projected designs of 1024x512 + 5 uneven ones), 4000
+   steps: batched gradient (one launch per step, CUDA graph) against the same
+   lattices one at a time.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, HERE)
+
+import lbmgpu as G  # noqa: E402
+import workloads as W  # noqa: E402
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import oracle
+    return oracle()
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def timed_gradient(cfg, gamma, n, k, reps=1):
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.init_equilibrium()
+        h.autotune(3)
+        h.gradient(min(n, 20), k)   # warm-up, allocates the slots
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            J, s, st = h.gradient(n, k)
+        dt = (time.perf_counter() - t0) / reps
+    return J, s, st, dt
+
+
+def step_rates(cfg, gamma, nsteps=50):
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.init_equilibrium()
+        h.autotune(3)
+        h.forward(10)
+        mf = h.time_steps(0, nsteps)
+        ma = h.time_steps(1, nsteps)
+    return cfg.ncells * nsteps / mf / 1e3, cfg.ncells * nsteps / ma / 1e3
+
+
+def config1(quick):
+    cfg, g, n = W.workload_config1()
+    orc = _oracle()
+    with G.Handle(cfg) as h:
+        h.set_design(g)
+        h.init_equilibrium()
+        t0 = time.perf_counter()
+        J = h.forward(n)
+        tf = time.perf_counter() - t0
+        f = h.populations()
+    fo, _, Jo = orc.forward(cfg, g, n)
+    Jg, s, st, tg = timed_gradient(cfg, g, n, 64)
+    return {"config": 1, "workload": "128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps",
+            "forward_s": tf, "gradient_s_64_snapshots": tg, "recomputed": st.recomputed_steps,
+            "J": J, "J_rel_err_vs_oracle": abs(J - Jo) / abs(Jo),
+            "populations_max_rel_err_vs_oracle": float(np.abs(f - fo).max() / np.abs(fo).max())}
+
+
+def config2(quick):
+    n = 2000 if quick else 20000
+    cfg64, g, _ = W.workload_config2(G.STORE_FP64, nsteps=n)
+    cfg32 = cfg64.replace(storage=G.STORE_FP32)
+    J64, s64, st, t64 = timed_gradient(cfg64, g, n, 64)
+    J32, s32, _, t32 = timed_gradient(cfg32, g, n, 64)
+    out = {"config": 2, "workload": "1024x512 D2Q9 BGK + Brinkman, unsteady inlet, dissipated "
+                                    "energy, %d steps, 64 device snapshots" % n,
+           "recomputed": st.recomputed_steps, "gradient_s_fp64": t64, "gradient_s_fp32": t32,
+           "speedup_fp32": t64 / t32, "J_fp64": J64, "J_fp32_rel_err": abs(J32 - J64) / abs(J64),
+           "dJdgamma_fp32_rel_l2_err": rel(s32, s64)}
+    mf, ma = step_rates(cfg32, g)
+    out.update(mlups_fwd_fp32=mf, mlups_adj_fp32=ma)
+    # central differences, FP64, one inlet period
+    nfd = 2000
+    cfd = cfg64.replace(obj_weight=1.0 / nfd)
+    _, sfd, _, _ = timed_gradient(cfd, g, nfd, 64)
+    rng = np.random.default_rng(W.SEED_BASE + 22)
+    cells = rng.choice(cfg64.ncells, size=4 if quick else 16, replace=False)
+    h_fd = 1e-6
+    worst = 0.0
+    with G.Handle(cfd) as h:
+        for c in cells:
+            vals = []
+            for sgn in (1.0, -1.0):
+                gg = g.copy()
+                gg[c] = min(max(gg[c] + sgn * h_fd, 0.0), 1.0)
+                h.set_design(gg)
+                h.init_equilibrium()
+                vals.append((h.forward(nfd), gg[c]))
+            fd = (vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1])
+            worst = max(worst, abs(fd - sfd[c]) / np.abs(sfd).max())
+    out.update(fd_cells=int(len(cells)), fd_steps=nfd, fd_h=h_fd, fd_max_err_rel_to_max_sens=worst)
+    # reference adjoint on the 128x64 cut-down
+    orc = _oracle()
+    ccut, gcut, _ = W.workload_config2(G.STORE_FP64, nx=128, ny=64, nsteps=2000)
+    Jc, sc, _, _ = timed_gradient(ccut, gcut, 2000, 64)
+    Jo, so = orc.gradient(ccut, gcut, 2000)
+    out.update(cutdown_J_rel_err=abs(Jc - Jo) / abs(Jo),
+               cutdown_dJdgamma_max_rel_err=float(np.abs(sc - so).max() / np.abs(so).max()))
+    return out
+
+
+def config3(quick):
+    out = {"config": 3, "workload": "256x128x128 D3Q19 MRT + Brinkman duct"}
+    for name, st in (("fp64", G.STORE_FP64), ("fp32", G.STORE_FP32), ("fp16", G.STORE_FP16)):
+        cfg, g, _ = W.workload_config3(st)
+        mf, ma = step_rates(cfg, g, 10 if st == G.STORE_FP64 else 50)
+        out["mlups_fwd_" + name] = mf
+        out["mlups_adj_" + name] = ma
+    cfg, g, _ = W.workload_config3(G.STORE_FP64, nx=64, ny=32, nz=32, nsteps=300)
+    J64, s64, _, _ = timed_gradient(cfg, g, 300, 32)
+    for name, st in (("fp32", G.STORE_FP32), ("fp16", G.STORE_FP16)):
+        J, s, _, _ = timed_gradient(cfg.replace(storage=st), g, 300, 32)
+        out["dJdgamma_rel_l2_err_%s_64x32x32_300_steps" % name] = rel(s, s64)
+        out["J_rel_err_%s" % name] = abs(J - J64) / abs(J64)
+    return out
+
+
+def config4(quick):
+    n = 2000 if quick else 10000
+    cfg64, g, _ = W.workload_config4(G.STORE_FP64, nsteps=n)
+    cfg32 = cfg64.replace(storage=G.STORE_FP32)
+    J64, s64, st, t64 = timed_gradient(cfg64, g, n, 64)
+    J32, s32, _, t32 = timed_gradient(cfg32, g, n, 64)
+    mf, ma = step_rates(cfg32, g)
+    return {"config": 4, "workload": "512x256 D2Q9 + D2Q5 thermal, heat flux, %d steps" % n,
+            "gradient_s_fp64": t64, "gradient_s_fp32": t32, "recomputed": st.recomputed_steps,
+            "J_fp64": J64, "J_fp32_rel_err": abs(J32 - J64) / abs(J64),
+            "dJdgamma_fp32_rel_l2_err": rel(s32, s64), "mlups_fwd_fp32": mf, "mlups_adj_fp32": ma}
+
+
+def config5(quick):
+    n = 400 if quick else 4000
+    insts, _ = W.workload_config5(G.STORE_FP32, nsteps=n)
+    cells = sum(c.ncells for c, _ in insts)
+    # one at a time
+    t_single = 0.0
+    Js = []
+    for cfg, g in insts:
+        J, s, st, dt = timed_gradient(cfg, g, n, 64)
+        t_single += dt
+        Js.append(J)
+    with G.Batch([c for c, _ in insts]) as b:
+        for i, (_, g) in enumerate(insts):
+            b[i].set_design(g)
+        shape = b.autotune(3)
+        b.gradient(n, 64, use_graph=True)          # capture + first replay
+        t0 = time.perf_counter()
+        J, sens, st = b.gradient(n, 64, use_graph=True)
+        t_batch = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        b.gradient(n, 64, use_graph=False)
+        t_eager = time.perf_counter() - t0
+    return {"config": 5, "workload": "8 D2Q9 lattices (3 projected 1024x512 + 256x128 .. 768x384), "
+                                     "FP32, %d steps, 64 snapshots each" % n,
+            "cells": cells, "batch_block_shape": list(shape),
+            "gradient_s_batched_graph": t_batch, "gradient_s_batched_no_graph": t_eager,
+            "gradient_s_one_at_a_time": t_single,
+            "aggregate_mlups_batched": cells * n / t_batch / 1e6,
+            "aggregate_mlups_one_at_a_time": cells * n / t_single / 1e6,
+            "max_J_rel_diff_batched_vs_single": float(max(abs(a - b) / abs(b) for a, b in zip(J, Js)))}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--configs", type=int, nargs="*", default=[1, 2, 3, 4, 5])
+    ap.add_argument("--quick", action="store_true", help="shorter horizons")
+    a = ap.parse_args()
+    fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5}
+    for c in a.configs:
+        t0 = time.perf_counter()
+        r = fns[c](a.quick)
+        r["wall_s"] = time.perf_counter() - t0
+        print(json.dumps(r), flush=True)
+
+
+if __name__ == "__main__":
+    main()
