@@ -372,6 +372,7 @@ def main():
     t1 = time.perf_counter()
     barrier(dist)
     grad_fp32_s = (t1 - t0) / e2e_runs
+    J32, s32 = float(Jbuf[0]), s_np.copy()
     grad_fp32_s = max_over_ranks(dist, grad_fp32_s)
     recomputed = int(st.recomputed_steps)
     e2e_value = total_cells * NSTEPS_GRAD / grad_fp32_s / 1e6
@@ -380,7 +381,9 @@ def main():
            "what": "lbm_set_design (host FP64 design) + lbm_gradient (5000 forward steps, "
                    "%d recomputed by Wang checkpointing in 64 device slots, 5000 adjoint "
                    "steps) + dJ/dgamma to host, per step" % recomputed,
-           "gradient_s": round(grad_fp32_s, 4)}
+           "gradient_s": round(grad_fp32_s, 4),
+           "forward_sweep_ms": round(float(st.forward_ms), 2),
+           "reverse_sweep_ms": round(float(st.reverse_ms), 2)}
     h.close()
 
     # FP64 storage: same gradient, for the FP32-vs-FP64 comparison
@@ -392,6 +395,10 @@ def main():
     t0 = time.perf_counter()
     one_gradient(h64)
     grad_fp64_s = time.perf_counter() - t0
+    J64, s64 = float(Jbuf[0]), s_np.copy()
+    grad_err = {"J_rel": abs(J32 - J64) / abs(J64),
+                "dJdgamma_rel_l2": float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64)),
+                "dJdgamma_max_rel": float(np.abs(s32 - s64).max() / np.abs(s64).max())}
     h64.set_design(gamma)
     h64.init_equilibrium()
     ms64 = h64.time_steps(2, max(10, args.steps // 4))
@@ -429,7 +436,8 @@ def main():
                       "fp64_mlups_fwd_adj": round(mlups64, 2),
                       "gradient_s_fp32": round(grad_fp32_s, 4),
                       "gradient_s_fp64": round(grad_fp64_s, 4),
-                      "gradient_speedup_fp32_vs_fp64": round(grad_fp64_s / grad_fp32_s, 3)},
+                      "gradient_speedup_fp32_vs_fp64": round(grad_fp64_s / grad_fp32_s, 3),
+                      "gradient_fp32_vs_fp64_full_size": grad_err},
         "e2e": e2e,
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),

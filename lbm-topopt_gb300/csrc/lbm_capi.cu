@@ -78,6 +78,7 @@ struct lbm_handle {
   float* bcprof_f[LBM_MAX_BC] = {};
   int t = 0;
   bool have_design = false, have_state = false, have_adjoint = false;
+  bool accumulate = false;   // objective sums over steps into the block partials
   int64_t launches = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::string err;
@@ -103,6 +104,24 @@ int fail(lbm_handle* h, int code, const char* fmt, ...) {
     cudaError_t e_ = (call);                                                               \
     if (e_ != cudaSuccess) return fail((h), LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
+
+// *out = sum of partial[0..n) in a fixed order (one block of 1024 threads):
+// the objective summed over time steps by the accumulating reductions.
+__global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict__ partial,
+                                                       long long n, double* __restrict__ out) {
+  __shared__ double sh[32];
+  double acc = 0.;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) tot += sh[w];
+    *out = tot;
+  }
+}
 
 size_t state_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->pop_bytes; }
 size_t adjoint_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->adj_bytes; }
@@ -224,6 +243,9 @@ KParams base_params(const lbm_handle* h, int t) {
   p.ny = c.ny;
   p.nz = h->dim == 3 ? c.nz : 1;
   p.P = h->P;
+  p.step = (unsigned)t;
+  p.key_fwd = step_key(p.step, kSaltForward);
+  p.key_adj = step_key(p.step, kSaltAdjoint);
   p.omega = c.omega;
   for (int i = 0; i < 8; ++i) p.mrt[i] = c.mrt[i];
   p.pbb_scale = c.interp_scale;
@@ -299,6 +321,7 @@ KParams base_params(const lbm_handle* h, int t) {
   mf.cv_diss = (float)md.cv_diss;
   p.partial = h->partial;
   p.counter = h->counter;
+  p.accumulate = h->accumulate ? 1 : 0;
   p.gamma = h->gamma;
   p.sens = h->sens;
   return p;
@@ -328,6 +351,24 @@ int ensure_stage(lbm_handle* h) {
   CUDA_OR_FAIL(h, cudaMalloc(&h->stage, (size_t)h->ncell * h->Q * sizeof(double)));
   return 0;
 }
+
+// Objective summed over time steps without a per-step reduction: zero the
+// block partials, let every step's reduction add into them, sum them once.
+int begin_accumulate(lbm_handle* h, cudaStream_t st) {
+  CUDA_OR_FAIL(h, cudaMemsetAsync(h->partial, 0, h->partial_cap * sizeof(double), st));
+  h->accumulate = true;
+  return 0;
+}
+int begin_accumulate(lbm_handle* h) { return begin_accumulate(h, h->stream); }
+
+int end_accumulate(lbm_handle* h, double* out, cudaStream_t st) {
+  h->accumulate = false;
+  k_sum_partials<<<1, 1024, 0, st>>>(h->partial, (long long)h->partial_cap, out);
+  h->launches++;
+  CUDA_OR_FAIL(h, cudaGetLastError());
+  return 0;
+}
+int end_accumulate(lbm_handle* h, double* out) { return end_accumulate(h, out, h->stream); }
 
 // Buffer b of a handle's state pool: 0 and 1 are the state buffers, 2 .. K+1
 // the checkpoint slots' (see StatePool).
@@ -616,17 +657,29 @@ int lbm_forward(lbm_handle* h, int nsteps, double* J_steps, double* J_sum) {
   bool obj = h->cfg.objective != LBM_OBJ_NONE;
   int rc = ensure_jcap(h, (size_t)nsteps);
   if (rc) return rc;
+  const bool sum_only = obj && !J_steps;
+  if (sum_only && (rc = begin_accumulate(h))) return rc;
   for (int k = 0; k < nsteps; ++k) {
     rc = forward_step(h, (obj && k > 0) ? h->jdev + (k - 1) : nullptr);
-    if (rc) return rc;
+    if (rc) {
+      h->accumulate = false;
+      return rc;
+    }
   }
   if (obj) {
     rc = objective_only(h, h->jdev + (nsteps - 1));
+    if (!rc && sum_only) rc = end_accumulate(h, h->jdev);
+    h->accumulate = false;
     if (rc) return rc;
   }
   rc = sync(h);
   if (rc) return rc;
-  if (obj) {
+  if (sum_only) {
+    double acc = 0.;
+    CUDA_OR_FAIL(h, cudaMemcpy(&acc, h->jdev, sizeof(double), cudaMemcpyDeviceToHost));
+    if (!std::isfinite(acc)) return fail(h, LBM_ERR_NONFINITE, "objective is not finite");
+    if (J_sum) *J_sum = acc;
+  } else if (obj) {
     std::vector<double> js((size_t)nsteps);
     CUDA_OR_FAIL(h, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
     double acc = 0.;
@@ -796,12 +849,16 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
     if ((rc = init_into(h, pool_buffer(h, out)))) return rc;
     pool.set_current(out);
   }
+  // J = sum_t F(f_t), summed in the block partials across the sweep
+  if (obj && (rc = begin_accumulate(h))) return rc;
   if ((rc = save(ws.make_checkpoint(0)))) return rc;
   for (int s = 0; s < nsteps; ++s) {
-    if ((rc = advance((obj && s >= 1) ? h->jdev + (s - 1) : nullptr))) return rc;
-    if ((rc = save(ws.make_checkpoint(s + 1)))) return rc;
+    if ((rc = advance((obj && s >= 1) ? h->jdev : nullptr))) break;
+    if ((rc = save(ws.make_checkpoint(s + 1)))) break;
   }
-  if (obj && (rc = objective_at(h, cur_buf(), h->jdev + (nsteps - 1)))) return rc;
+  if (!rc && obj && !(rc = objective_at(h, cur_buf(), h->jdev))) rc = end_accumulate(h, h->jdev);
+  h->accumulate = false;
+  if (rc) return rc;
   cudaEventRecord(h->ev[1], h->stream);
   if ((rc = zero_adjoint(h))) return rc;
   h->have_adjoint = true;
@@ -825,9 +882,7 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
   if ((rc = sync(h))) return rc;
   double acc = 0.;
   if (obj) {
-    std::vector<double> js((size_t)nsteps);
-    CUDA_OR_FAIL(h, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (double v : js) acc += v;
+    CUDA_OR_FAIL(h, cudaMemcpy(&acc, h->jdev, sizeof(double), cudaMemcpyDeviceToHost));
     if (!std::isfinite(acc)) return fail(h, LBM_ERR_NONFINITE, "objective is not finite");
   }
   if (J) *J = acc;
@@ -1202,14 +1257,32 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
     if ((rc = batch_init(b, out))) return rc;
     pool.set_current(out);
   }
-  if ((rc = save(ws.make_checkpoint(0)))) return rc;
-  for (int s = 0; s < nsteps; ++s) {
-    for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev + (s - 1) : nullptr;
-    if ((rc = advance(res))) return rc;
-    if ((rc = save(ws.make_checkpoint(s + 1)))) return rc;
+  // J of every lattice summed in its block partials across the sweep
+  for (int i = 0; i < b->n; ++i)
+    if (b->h[i]->cfg.objective != LBM_OBJ_NONE && (rc = begin_accumulate(b->h[i], b->stream)))
+      return bfail(b, rc, "%s", b->h[i]->err.c_str());
+  auto stop_accumulating = [&]() {
+    for (int i = 0; i < b->n; ++i) b->h[i]->accumulate = false;
+  };
+  if ((rc = save(ws.make_checkpoint(0)))) {
+    stop_accumulating();
+    return rc;
   }
-  for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev + (nsteps - 1);
-  if ((rc = batch_objective(b, pool.current(), res))) return rc;
+  for (int s = 0; s < nsteps; ++s) {
+    for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev : nullptr;
+    if ((rc = advance(res)) || (rc = save(ws.make_checkpoint(s + 1)))) {
+      stop_accumulating();
+      return rc;
+    }
+  }
+  for (int i = 0; i < b->n; ++i) res[i] = b->h[i]->jdev;
+  rc = batch_objective(b, pool.current(), res);
+  for (int i = 0; i < b->n && !rc; ++i)
+    if (b->h[i]->cfg.objective != LBM_OBJ_NONE &&
+        (rc = end_accumulate(b->h[i], b->h[i]->jdev, b->stream)))
+      rc = bfail(b, rc, "%s", b->h[i]->err.c_str());
+  stop_accumulating();
+  if (rc) return rc;
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     for (void* p : h->lam) BCUDA(b, cudaMemsetAsync(p, 0, adjoint_bytes(h), b->stream));
@@ -1483,13 +1556,12 @@ int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, doubl
   BCUDA(b, cudaStreamSynchronize(b->stream));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
-  std::vector<double> js((size_t)nsteps);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     if (J) {
-      BCUDA(b, cudaMemcpy(js.data(), h->jdev, js.size() * sizeof(double), cudaMemcpyDeviceToHost));
       double acc = 0.;
-      for (double v : js) acc += v;
+      if (h->cfg.objective != LBM_OBJ_NONE)
+        BCUDA(b, cudaMemcpy(&acc, h->jdev, sizeof(double), cudaMemcpyDeviceToHost));
       if (!std::isfinite(acc)) return bfail(b, LBM_ERR_NONFINITE, "lattice %d: objective not finite", i);
       J[i] = acc;
     }

@@ -132,8 +132,10 @@ template <>
 struct Store<float> {
   using C = float;
   static constexpr bool SHIFT = true;
-  __device__ static C ld(const float* p) { return __ldcs(p); }
-  __device__ static void st(float* p, C v) { __stcs(p, v); }
+  // Plain cached accesses: on GB300 the evict-first (.cs) forms of these
+  // loads and stores cut a 19-plane streaming copy from 6.5 to 4.0 TB/s.
+  __device__ static C ld(const float* p) { return *p; }
+  __device__ static void st(float* p, C v) { *p = v; }
 };
 
 template <>
@@ -208,6 +210,8 @@ struct ModelParams {
 struct KParams {
   int nx, ny, nz;
   long long P;       // plane stride in elements
+  unsigned step;     // time step of the input state
+  unsigned key_fwd, key_adj;   // rounding-stream keys of the two step kernels at this step
   // model
   double omega;
   double mrt[8];
@@ -222,6 +226,7 @@ struct KParams {
   // objective
   int objective;
   int eval_obj;
+  int accumulate;          // add each block's sum to partial[block] (no counter, no result)
   double obj_weight, inv_in, inv_out;
   int obj_in[6], obj_out[6];
   double* partial;         // per-block partial sums
@@ -960,6 +965,241 @@ __device__ __forceinline__ void thermal_collide(C* gp, C ux, C uy, C g, C& T, co
   });
 }
 
+// ---------------------------------------------------------------------------
+// Collision in increment form, for FP32 and FP16 storage.
+//
+// Rounding to nearest is deterministic: in a slowly varying flow a cell rounds
+// the same way at every step, which acts like a small constant source of mass
+// and momentum, and the stored state drifts away from the exact one linearly
+// in time (4e-4 relative after 20000 steps of a 1024x512 channel in FP32).
+// Two changes remove the drift:
+//  - the collision produces increments d (f_out = f + d) whose mass and
+//    momentum change is exactly the operator's (zero, except the partial
+//    bounce-back drag) up to the rounding of d itself, which is orders of
+//    magnitude below that of f: BGK increments are projected onto zero mass and
+//    momentum, MRT increments are back-mapped from the non-conserved moments
+//    only, and the partial bounce-back moves equal and opposite amounts;
+//  - f + d is rounded to the storage type without bias (stochastic rounding:
+//    uniform noise of one unit in the last place is added before rounding to
+//    nearest), keyed on (cell, time step, direction), so a recomputed step
+//    reproduces its state bit for bit.
+
+__host__ __device__ __forceinline__ unsigned mix32(unsigned v) {
+  v ^= v >> 16;
+  v *= 0x7feb352du;
+  v ^= v >> 15;
+  v *= 0x846ca68bu;
+  v ^= v >> 16;
+  return v;
+}
+
+// Per-cell stream of uniform variates: a hash of (cell, step, salt) seeds a
+// 32-bit linear congruential sequence whose top 23 bits are used.
+struct Dither {
+  unsigned r;
+  // key: step_key(step, salt), the same for every cell of a launch
+  __device__ __forceinline__ Dither(unsigned cell, unsigned key) : r(mix32(cell ^ key)) {}
+  // uniform in [-1/2, 1/2) * 2^-K for K = 23 (FP32) or 10 (FP16)
+  template <int K>
+  __device__ __forceinline__ float next() {
+    r = r * 1664525u + 1013904223u;
+    constexpr unsigned kExp = (unsigned)(127 - K) << 23;
+    constexpr float kHalf = 1.5f / (float)(1u << K);
+    return __uint_as_float(kExp | (r >> 9)) - kHalf;
+  }
+};
+
+// Salts of the rounding streams of the two step kernels.
+constexpr unsigned kSaltForward = 0x85ebca6bu, kSaltAdjoint = 0xc2b2ae35u;
+
+__host__ __device__ __forceinline__ unsigned step_key(unsigned step, unsigned salt) {
+  return mix32(step * 0x9E3779B9u + salt);
+}
+
+// Largest power of two not above |v| (0 for zero and subnormals).
+__device__ __forceinline__ float pow2_floor(float v) {
+  return __uint_as_float(__float_as_uint(v) & 0x7f800000u);
+}
+
+template <class S>
+struct Round;
+template <>
+struct Round<float> {
+  // The noise is scaled to the unit in the last place of f; where f + d
+  // leaves f's binade (|d| is mostly far below |f|) the rounding is still
+  // unbiased downwards and nearly so upwards.
+  __device__ static __forceinline__ float apply(float f, float d, Dither& rnd) {
+    return f + fmaf(rnd.next<23>(), pow2_floor(f), d);
+  }
+};
+template <>
+struct Round<__half> {
+  __device__ static __forceinline__ __half apply(float f, float d, Dither& rnd) {
+    const float s = f + d;
+    // below 2^-14 the FP16 spacing stays 2^-24 (subnormals)
+    const float bin = fmaxf(pow2_floor(s), 6.103515625e-05f);
+    return __float2half_rn(fmaf(rnd.next<10>(), bin, s));
+  }
+};
+
+// sum_a e_ia j_a with the zero terms left out
+template <int LAT, int i, class C>
+__device__ __forceinline__ C e_dot(C jx, C jy, C jz) {
+  using L = Lattice<LAT>;
+  C v = C(0.);
+  if constexpr (L::ex(i) == 1) v += jx;
+  if constexpr (L::ex(i) == -1) v -= jx;
+  if constexpr (L::ey(i) == 1) v += jy;
+  if constexpr (L::ey(i) == -1) v -= jy;
+  if constexpr (L::ez(i) == 1) v += jz;
+  if constexpr (L::ez(i) == -1) v -= jz;
+  return v;
+}
+
+// d_i -= w_i (sum d + 3 e_i . sum e d): the increments then carry no mass and
+// no momentum (sum w = 1, sum w e = 0, sum w e e = I/3).
+template <int LAT, class C>
+__device__ __forceinline__ void project_conserved(C* d) {
+  using L = Lattice<LAT>;
+  C a = C(0.), bx = C(0.), by = C(0.), bz = C(0.);
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    a += d[i];
+    if constexpr (L::ex(i) == 1) bx += d[i];
+    if constexpr (L::ex(i) == -1) bx -= d[i];
+    if constexpr (L::ey(i) == 1) by += d[i];
+    if constexpr (L::ey(i) == -1) by -= d[i];
+    if constexpr (L::ez(i) == 1) bz += d[i];
+    if constexpr (L::ez(i) == -1) bz -= d[i];
+  });
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    d[i] -= C(L::w(i)) * (a + C(3.) * e_dot<LAT, i>(bx, by, bz));
+  });
+}
+
+// Increments of mrt3d_pair_collide (same operator: f + d is its output),
+// handed to emit(q, d_q) pair by pair so each pair's registers are freed early.
+template <class C, class Emit>
+__device__ __forceinline__ void mrt3d_pair_collide_inc(const C* f, C imult, C& rho, C& jx, C& jy,
+                                                       C& jz, const KParams& p, Emit&& emit) {
+  C s[10], a[10], mo[15];
+  mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, mo);
+  mrt3d_relax(mo, rho, jx, jy, jz, p);
+  C d0 = C(0.);
+  static_for<15>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    constexpr int c = mrt3d_m(k, 0);
+    if constexpr (mrt3d_even(k) && c != 0) {
+      constexpr double b = -(double)c / (double)mrt3d_n(k);
+      d0 += C(b) * mo[k];
+    }
+  });
+  emit(std::integral_constant<int, 0>{}, d0);
+  const C twoim = C(2.) * imult;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    C E = C(0.), O = C(0.);
+    static_for<15>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      constexpr int c = mrt3d_m(k, d);
+      if constexpr (c != 0) {
+        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
+        if constexpr (mrt3d_even(k))
+          E += C(b) * mo[k];
+        else
+          O += C(b) * mo[k];
+      }
+    });
+    // s' = s + E, a'' = (a + O)(1 - 2 imult) = a + O - 2 imult (a + O); a is
+    // recomputed from f (same value) so that only f stays live across the loop
+    const C da = O - twoim * ((f[d] - f[d + 9]) + O);
+    emit(std::integral_constant<int, d>{}, C(0.5) * (E + da));
+    emit(std::integral_constant<int, d + 9>{}, C(0.5) * (E - da));
+  });
+}
+
+// Increments of flow_collide (collision + partial bounce-back), handed to
+// emit(q, d_q) once per flow population; returns the macros of the input.
+template <int LAT, int COLL, class C, class Emit>
+__device__ __forceinline__ void flow_collide_inc(const C* f, C imult, C& rho, C& jx, C& jy, C& jz,
+                                                 const KParams& p, Emit&& emit) {
+  using L = Lattice<LAT>;
+  if constexpr (LAT == LAT_D3Q19 && COLL == LBM_MRT) {
+    mrt3d_pair_collide_inc(f, imult, rho, jx, jy, jz, p, emit);
+  } else {
+    C d[L::QF];
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    if constexpr (COLL == LBM_BGK) {
+      const C om = mp<C>(p).omega;
+      const C uSqr = jx * jx + jy * jy + jz * jz;
+      const C cFeq = rho - C(1.5) * uSqr;
+      static_for<L::QF>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        const C sc = e_dot<LAT, i>(jx, jy, jz);
+        const C eq = C(L::w(i)) * (cFeq + C(3.) * sc + C(4.5) * sc * sc);
+        d[i] = om * (eq - f[i]);
+      });
+      project_conserved<LAT>(d);
+    } else {
+      using M = MRT<L::DIM>;
+      C mo[M::K];
+      mrt_moments<L::DIM>(f, mo);
+      if (L::DIM == 2)
+        mrt2d_relax(mo, rho, jx, jy, p);
+      else
+        mrt3d_relax(mo, rho, jx, jy, jz, p);
+      static_for<M::QF>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        C v = C(0.);
+        static_for<M::K>([&](auto KK) {
+          constexpr int k = decltype(KK)::value;
+          constexpr int c = M::m(k, i);
+          if constexpr (c != 0) {
+            constexpr double b = -(double)c / (double)M::n(k);
+            v += C(b) * mo[k];
+          }
+        });
+        d[i] = v;
+      });
+    }
+    emit(std::integral_constant<int, 0>{}, d[0]);
+    // partial bounce-back on the collided values f + d, moving equal and
+    // opposite amounts within each pair
+    static_for<L::HALF>([&](auto D) {
+      constexpr int k = decltype(D)::value + 1;
+      const C m = imult * ((f[k + L::HALF] - f[k]) + (d[k + L::HALF] - d[k]));
+      emit(std::integral_constant<int, k>{}, d[k] + m);
+      emit(std::integral_constant<int, k + L::HALF>{}, d[k + L::HALF] - m);
+    });
+  }
+}
+
+// Increments of thermal_collide, handed to emit(i, d_i) for i = 0..4: the
+// collision conserves sum g up to the rounding of the increments; the heating
+// source is added after.
+template <class C, class Emit>
+__device__ __forceinline__ void thermal_collide_inc(const C* gp, C ux, C uy, C g, const KParams& p,
+                                                    Emit&& emit) {
+  using L = Lattice<LAT_D2Q9_D2Q5>;   // D2Q5 directions are its entries 9..13
+  const C om = thermal_omega(g, p);
+  const C T = gp[0] + gp[1] + gp[2] + gp[3] + gp[4];
+  const C hs = (C(1.) - g) * mp<C>(p).heat_rate * (mp<C>(p).heat_T - T);
+  C dg[5];
+  C a = C(0.);
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const C sc = e_dot<LAT_D2Q9_D2Q5, i + 9>(ux, uy, C(0.));
+    const C eq = C(L::w(i + 9)) * T * (C(1.) + C(3.) * sc);
+    dg[i] = om * (eq - gp[i]);
+    a += dg[i];
+  });
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    emit(I, dg[i] + C(L::w(i + 9)) * (hs - a));
+  });
+}
+
 // Transpose of thermal_collide at input (gin, ux, uy); lam[0..4] in/out;
 // returns the adjoint of (ux, uy) and adds to dg.
 template <class C>
@@ -991,6 +1231,144 @@ __device__ __forceinline__ void thermal_reverse(const C* gin, C* lam, C ux, C uy
   dg += omR * (C(-1.) / (den * den)) * C(3.) * mp<C>(p).diff * ramp_diff(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck);
 #pragma unroll
   for (int i = 0; i < 5; ++i) lam[i] = li[i] + TR;
+}
+
+// Increments d[0..4] of thermal_reverse: lam + d is its output; the same
+// adjoint of (ux, uy) and the same dg.  The constant vector is invariant under
+// the transposed collision (sum_j dgeq_j/dT = 1), so the increment is projected
+// with c = sum_i W_i (1 + 3 e_i . u) d_i before the heating term is added.
+template <class C>
+__device__ __forceinline__ void thermal_reverse_inc(const C* gin, const C* lam, C* d, C ux, C uy,
+                                                    C g, C& uxR, C& uyR, C& dg, const KParams& p) {
+  using L = Lattice<LAT_D2Q9_D2Q5>;   // D2Q5 directions are its entries 9..13
+  const C T = gin[0] + gin[1] + gin[2] + gin[3] + gin[4];
+  const C om = thermal_omega(g, p);
+  C cT = C(0.), omR = C(0.), hsR = C(0.);
+  uxR = C(0.);
+  uyR = C(0.);
+  C wt[5];
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const C sc = e_dot<LAT_D2Q9_D2Q5, i + 9>(ux, uy, C(0.));
+    const C w = C(L::w(i + 9));
+    const C eq = w * T * (C(1.) + C(3.) * sc);
+    wt[i] = w * (C(1.) + C(3.) * sc);
+    cT += wt[i] * lam[i];
+    omR += (eq - gin[i]) * lam[i];
+    const C a = om * lam[i] * w;
+    if constexpr (L::ex(i + 9) != 0) uxR += a * T * C(3. * L::ex(i + 9));
+    if constexpr (L::ey(i + 9) != 0) uyR += a * T * C(3. * L::ey(i + 9));
+    hsR += w * lam[i];
+  });
+  C c = C(0.);
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    d[i] = om * (cT - lam[i]);
+    c += wt[i] * d[i];
+  });
+  const C heat = -(C(1.) - g) * mp<C>(p).heat_rate * hsR;
+  static_for<5>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    d[i] = (d[i] - c) + heat;
+  });
+  dg += -mp<C>(p).heat_rate * (mp<C>(p).heat_T - T) * hsR;
+  const C den = C(3.) * mp<C>(p).diff * ramp(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck) + C(0.5);
+  dg += omR * (C(-1.) / (den * den)) * C(3.) * mp<C>(p).diff *
+        ramp_diff(g, mp<C>(p).ramp_q, mp<C>(p).ramp_ck);
+}
+
+
+// ---------------------------------------------------------------------------
+// Reverse BGK and thermal collisions in increment form (FP32 adjoints).
+//
+// The transpose of a BGK collision at state f is lam -> mu + omega (E^T mu - mu)
+// with mu the reverse partial bounce-back of lam and E the Jacobian of the
+// equilibrium, a projection (E^2 = E) whose transpose keeps the constant
+// vector and e_a: these directions are invariant, so rounding errors along
+// them add up over the reverse sweep exactly as mass and momentum errors do in
+// the forward one.  The increments are projected with (I - E^T), which keeps
+// the exact increment unchanged and removes those components, and lam + d is
+// rounded without bias (Round / Dither).
+
+// (E^T v)_i = c0 + e_i . c with c0 = sum_j w_j v_j and
+// c_a = sum_j w_j (3 e_ja + 9 (e_j . u) e_ja - 3 u_a) v_j (incompressible
+// equilibrium at velocity u = j).
+template <int LAT, class C>
+__device__ __forceinline__ void eq_transpose_coeffs(const C* v, C jx, C jy, C jz, C& c0, C& cx,
+                                                    C& cy, C& cz) {
+  using L = Lattice<LAT>;
+  C p1x = C(0.), p1y = C(0.), p1z = C(0.), p2x = C(0.), p2y = C(0.), p2z = C(0.);
+  c0 = C(0.);
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const C wv = C(L::w(i)) * v[i];
+    const C sw = e_dot<LAT, i>(jx, jy, jz) * wv;
+    c0 += wv;
+    if constexpr (L::ex(i) == 1) { p1x += wv; p2x += sw; }
+    if constexpr (L::ex(i) == -1) { p1x -= wv; p2x -= sw; }
+    if constexpr (L::ey(i) == 1) { p1y += wv; p2y += sw; }
+    if constexpr (L::ey(i) == -1) { p1y -= wv; p2y -= sw; }
+    if constexpr (L::ez(i) == 1) { p1z += wv; p2z += sw; }
+    if constexpr (L::ez(i) == -1) { p1z -= wv; p2z -= sw; }
+  });
+  cx = C(3.) * (p1x - jx * c0) + C(9.) * p2x;
+  cy = C(3.) * (p1y - jy * c0) + C(9.) * p2y;
+  cz = C(3.) * (p1z - jz * c0) + C(9.) * p2z;
+}
+
+// Increments d of flow_reverse<LAT, BGK> at input fin: lam + d is its output;
+// dg += dimult * d(out)/d(imult)^T lam.
+template <int LAT, class C>
+__device__ __forceinline__ void bgk_reverse_inc(const C* fin, const C* lam, C* d, C imult,
+                                                C dimult, C& dg, const KParams& p) {
+  using L = Lattice<LAT>;
+  constexpr int H = L::HALF;
+  C rho, jx, jy, jz;
+  flow_macros<LAT>(fin, rho, jx, jy, jz);
+  const C om = mp<C>(p).omega;
+  const C cFeq = rho - C(1.5) * (jx * jx + jy * jy + jz * jz);
+  // sensitivity to imult: sum over pairs of (fo_k - fo_opp)(lam_opp - lam_k),
+  // fo the collided state before partial bounce-back
+  C imultRev = C(0.);
+  static_for<H>([&](auto D) {
+    constexpr int k = decltype(D)::value + 1;
+    const C sk = e_dot<LAT, k>(jx, jy, jz), so = e_dot<LAT, k + H>(jx, jy, jz);
+    const C fok = fin[k] + om * (C(L::w(k)) * (cFeq + C(3.) * sk + C(4.5) * sk * sk) - fin[k]);
+    const C foo = fin[k + H] + om * (C(L::w(k + H)) * (cFeq + C(3.) * so + C(4.5) * so * so) - fin[k + H]);
+    imultRev += (fok - foo) * (lam[k + H] - lam[k]);
+  });
+  dg += dimult * imultRev;
+  // reverse partial bounce-back: mu = lam + m, m_k = imult (lam_opp - lam_k),
+  // recomputed where needed instead of held in registers
+  auto mpbb = [&](auto I) -> C {
+    constexpr int i = decltype(I)::value;
+    if constexpr (i == 0 || i > L::QF - 1) {
+      return C(0.);
+    } else if constexpr (i <= H) {
+      return imult * (lam[i + H] - lam[i]);
+    } else {
+      return -(imult * (lam[i] - lam[i - H]));
+    }
+  };
+  // reverse collision: omega (E^T mu - mu), projected with (I - E^T)
+  C c0, cx, cy, cz;
+  {
+    C mu[L::QF];
+    static_for<L::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      mu[i] = lam[i] + mpbb(I);
+    });
+    eq_transpose_coeffs<LAT>(mu, jx, jy, jz, c0, cx, cy, cz);
+    static_for<L::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      d[i] = om * (c0 + e_dot<LAT, i>(cx, cy, cz) - mu[i]);
+    });
+  }
+  eq_transpose_coeffs<LAT>(d, jx, jy, jz, c0, cx, cy, cz);
+  static_for<L::QF>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    d[i] = (d[i] - (c0 + e_dot<LAT, i>(cx, cy, cz))) + mpbb(I);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -1332,6 +1710,21 @@ __device__ __forceinline__ void grid_reduce_v(C v, const KParams& p, unsigned bi
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nthr = blockDim.x * blockDim.y;
+  if (p.accumulate) {
+    // Sum over time steps: every block adds its own sum to its own slot, so
+    // no counter, fence or atomic is needed; blocks whose cells contribute
+    // nothing (e.g. away from the pressure-drop strips) stop here.
+    if (!__syncthreads_or(v != C(0.))) return;
+    v = warp_sum(v);
+    if ((tid & 31) == 0) sh[tid >> 5] = (double)v;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.;
+      for (int w = 0; w < (nthr + 31) / 32; ++w) s += sh[w];
+      p.partial[bid] += s;
+    }
+    return;
+  }
   __syncthreads();   // the shared slots may still be read from a previous call
   // warps whose cells contribute nothing (e.g. away from the pressure-drop
   // strips) skip the shuffle tree

@@ -22,15 +22,18 @@ namespace lbm {
 
 // Resident 256-thread blocks per SM requested from the compiler (register
 // cap).  The FP32/FP16 step kernels are HBM-bound and need the warps to keep
-// enough loads in flight: 4 blocks (64 registers) measured fastest for the
-// D3Q19 adjoint; the FP64 kernels are FP64-throughput-bound on GB300 and keep
-// all their registers.
-template <class S>
+// enough loads in flight: 5 blocks (48 registers) measured fastest for the
+// D3Q19 MRT forward step and 4 (64 registers) for its adjoint; the D3Q19 BGK
+// adjoint in increment form needs more registers than 64 and gets 3 blocks
+// (85); the FP64 kernels are FP64-throughput-bound on GB300 and keep all
+// their registers.
+template <int LAT, int COLL, class S>
 struct Occupancy {
-  static constexpr int fwd = 4, adj = 4;
+  static constexpr int fwd = 5;
+  static constexpr int adj = (LAT == LAT_D3Q19 && COLL == LBM_BGK) ? 3 : 4;
 };
-template <>
-struct Occupancy<double> {
+template <int LAT, int COLL>
+struct Occupancy<LAT, COLL, double> {
   static constexpr int fwd = 1, adj = 1;
 };
 
@@ -107,23 +110,33 @@ __device__ __forceinline__ typename Store<S>::C from_abs(double v) {
 
 // Push f[q] of cell c to its neighbour (or bounce it back into opp(q) of c).
 // Interior cells take one branch with no per-direction tests.
-template <int LAT, class S>
-__device__ __forceinline__ void push_all(const typename Store<S>::C* f, S* __restrict__ fout,
-                                         int c, int x, int y, int z, bool in, const KParams& p) {
+// Values are either in the compute type (converted on store) or already in
+// the storage type.
+template <class S, class V>
+__device__ __forceinline__ void put(S* ptr, V v) {
+  if constexpr (std::is_same<S, V>::value)
+    *ptr = v;
+  else
+    Store<S>::st(ptr, v);
+}
+
+template <int LAT, class S, class V>
+__device__ __forceinline__ void push_all(const V* f, S* __restrict__ fout, int c, int x, int y,
+                                         int z, bool in, const KParams& p) {
   using L = Lattice<LAT>;
   const int P = (int)p.P, sx = p.nx, sxy = p.nx * p.ny;
   if (in) {
     static_for<L::Q>([&](auto Q_) {
       constexpr int q = decltype(Q_)::value;
-      Store<S>::st(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
+      put(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
     });
   } else {
     static_for<L::Q>([&](auto Q_) {
       constexpr int q = decltype(Q_)::value;
       if (nb_inside<LAT, q>(x, y, z, p))
-        Store<S>::st(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
+        put(fout + (q * P + c + nb_offset<LAT, q>(sx, sxy)), f[q]);
       else
-        Store<S>::st(fout + (L::opp(q) * P + c), f[q]);
+        put(fout + (L::opp(q) * P + c), f[q]);
     });
   }
 }
@@ -173,12 +186,28 @@ __device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, i
     if (p.eval_obj) objv = objective_cell<LAT, SHIFT>(f, g, x, y, z, p);
     const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C rho, jx, jy, jz;
-    flow_collide<LAT, COLL>(f, imult, rho, jx, jy, jz, p);
-    if (LAT == LAT_D2Q9_D2Q5) {
-      C T;
-      thermal_collide(f + 9, jx, jy, g, T, p);
+    if constexpr (SHIFT) {
+      // FP32/FP16 storage: increments, rounded to the storage type without bias
+      Dither rnd((unsigned)c, p.key_fwd);
+      S o[L::Q];
+      flow_collide_inc<LAT, COLL>(f, imult, rho, jx, jy, jz, p, [&](auto Q_, C dq) {
+        constexpr int q = decltype(Q_)::value;
+        o[q] = Round<S>::apply(f[q], dq, rnd);
+      });
+      if constexpr (LAT == LAT_D2Q9_D2Q5)
+        thermal_collide_inc(f + 9, jx, jy, g, p, [&](auto I_, C dq) {
+          constexpr int q = decltype(I_)::value + 9;
+          o[q] = Round<S>::apply(f[q], dq, rnd);
+        });
+      push_all<LAT, S>(o, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
+    } else {
+      flow_collide<LAT, COLL>(f, imult, rho, jx, jy, jz, p);
+      if (LAT == LAT_D2Q9_D2Q5) {
+        C T;
+        thermal_collide(f + 9, jx, jy, g, T, p);
+      }
+      push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
     }
-    push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
   }
   return objv;
 }
@@ -205,6 +234,42 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
   const C dimult = C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q));
   C dg = C(0.);
   C uxR = C(0.), uyR = C(0.);
+  if constexpr (SHIFT && COLL == LBM_BGK) {
+    // FP32 adjoints: increments, rounded without bias away from the boundary faces
+    C d[L::Q];
+    if constexpr (LAT == LAT_D2Q9_D2Q5) {
+      C rho, jx, jy, jz;
+      flow_macros<LAT>(f, rho, jx, jy, jz);
+      thermal_reverse_inc(f + 9, lam + 9, d + 9, jx, jy, g, uxR, uyR, dg, p);
+    }
+    bgk_reverse_inc<LAT>(f, lam, d, imult, dimult, dg, p);
+    if constexpr (LAT == LAT_D2Q9_D2Q5) {
+      static_for<9>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        d[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+      });
+    }
+    if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, d, dg, x, y, z, p);
+    if (on_bc_face(x, p)) {
+      static_for<L::Q>([&](auto Q_) {
+        constexpr int q = decltype(Q_)::value;
+        lam[q] += d[q];
+      });
+      adjoint_bcs<LAT>(lam, x, y, z, p);
+      static_for<L::Q>([&](auto Q_) {
+        constexpr int q = decltype(Q_)::value;
+        lout[q * (int)p.P + c] = A(lam[q]);
+      });
+    } else {
+      Dither rnd((unsigned)c, p.key_adj);
+      static_for<L::Q>([&](auto Q_) {
+        constexpr int q = decltype(Q_)::value;
+        lout[q * (int)p.P + c] = Round<A>::apply(lam[q], d[q], rnd);
+      });
+    }
+    p.sens[c] += (double)dg;
+    return;
+  }
   if (LAT == LAT_D2Q9_D2Q5) {
     C rho, jx, jy, jz;
     flow_macros<LAT>(f, rho, jx, jy, jz);
@@ -246,7 +311,7 @@ __device__ __forceinline__ typename Store<S>::C objective_only_cell(const KParam
 }
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
+__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd) k_forward(KParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const auto objv = forward_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
@@ -254,7 +319,7 @@ __global__ void __launch_bounds__(256, Occupancy<S>::fwd) k_forward(KParams p) {
 }
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::adj) k_adjoint(KParams p) {
+__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj) k_adjoint(KParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   adjoint_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
@@ -276,7 +341,7 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
 // parameters are read in place from the launch's parameter space.
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::fwd)
+__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     k_forward_batch(const __grid_constant__ BatchParams bp) {
   for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
     int i = 0;
@@ -292,7 +357,7 @@ __global__ void __launch_bounds__(256, Occupancy<S>::fwd)
 }
 
 template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<S>::adj)
+__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj)
     k_adjoint_batch(const __grid_constant__ BatchParams bp) {
   for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
     int i = 0;

@@ -119,6 +119,9 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
   p.ny = c.ny;
   p.nz = nz;
   p.P = P;
+  p.step = (unsigned)t;
+  p.key_fwd = step_key(p.step, kSaltForward);
+  p.key_adj = step_key(p.step, kSaltAdjoint);
   ModelParams<double>& md = p.md;
   md.omega = c.omega;
   for (int i = 0; i < 8; ++i) md.mrt[i] = c.mrt[i];

@@ -18,10 +18,13 @@ static lbm_dim3_stub threadIdx, blockIdx, blockDim, gridDim;
 template <class T> T __shfl_down_sync(unsigned, T v, int) { return v; }
 inline int __any_sync(unsigned, int v) { return v; }
 inline void __syncthreads() {}
+inline int __syncthreads_or(int v) { return v; }
 inline void __threadfence() {}
 inline unsigned atomicAdd(unsigned* p, unsigned v) { unsigned o = *p; *p += v; return o; }
 inline float __ldcs(const float* p) { return *p; }
 inline void __stcs(float* p, float v) { *p = v; }
+inline float __uint_as_float(unsigned u) { float f; memcpy(&f, &u, 4); return f; }
+inline unsigned __float_as_uint(float f) { unsigned u; memcpy(&u, &f, 4); return u; }
 #include "../lbm-topopt_gb300/csrc/lbm_device.cuh"
 
 using namespace lbm;
@@ -96,6 +99,86 @@ void reverse(const lbm_config* cfg, const double* fin, double g, const double* l
   *dgo = (double)dg;
 }
 
+// f + d from the increment form of the collision (FP32/FP16 storage path)
+template <int LAT, int COLL, class C>
+void collide_inc(const lbm_config* cfg, const double* fin, double g, double* fout, double* sums) {
+  KParams p;
+  fill<C>(p, cfg);
+  using L = Lattice<LAT>;
+  constexpr int Q = L::Q;
+  C f[Q], d[Q];
+  for (int i = 0; i < Q; ++i) f[i] = (C)fin[i];
+  const C gg = (C)g;
+  const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(gg, mp<C>(p).pbb_q));
+  C rho, jx, jy, jz;
+  flow_collide_inc<LAT, COLL>(f, imult, rho, jx, jy, jz, p, [&](auto Q_, C dq) {
+    d[decltype(Q_)::value] = dq;
+  });
+  if constexpr (LAT == LAT_D2Q9_D2Q5)
+    thermal_collide_inc(f + 9, jx, jy, gg, p, [&](auto I_, C dq) { d[decltype(I_)::value + 9] = dq; });
+  for (int i = 0; i < Q; ++i) fout[i] = (double)f[i] + (double)d[i];
+  // mass and momentum of the flow increments, and the largest increment
+  double m[5] = {0., 0., 0., 0., 0.};
+  for (int i = 0; i < L::QF; ++i) {
+    m[0] += (double)d[i];
+    m[1] += L::ex(i) * (double)d[i];
+    m[2] += L::ey(i) * (double)d[i];
+    m[3] += L::ez(i) * (double)d[i];
+    m[4] = fmax(m[4], fabs((double)d[i]));
+  }
+  for (int k = 0; k < 5; ++k) sums[k] = m[k];
+}
+
+// lo + d from the increment form of the BGK / thermal reverse collision
+template <int LAT, class C>
+void reverse_inc(const lbm_config* cfg, const double* fin, double g, const double* lo, double* li,
+                 double* dgo) {
+  KParams p;
+  fill<C>(p, cfg);
+  using L = Lattice<LAT>;
+  constexpr int Q = L::Q;
+  C f[Q], lam[Q], d[Q];
+  for (int i = 0; i < Q; ++i) {
+    f[i] = (C)fin[i];
+    lam[i] = (C)lo[i];
+  }
+  const C gg = (C)g;
+  const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(gg, mp<C>(p).pbb_q));
+  const C dimult = C(0.5) * (mp<C>(p).pbb_scale * bp_diff(gg, mp<C>(p).pbb_q));
+  C dg = C(0.), uxR = C(0.), uyR = C(0.);
+  if constexpr (LAT == LAT_D2Q9_D2Q5) {
+    C rho, jx, jy, jz;
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    thermal_reverse_inc(f + 9, lam + 9, d + 9, jx, jy, gg, uxR, uyR, dg, p);
+  }
+  bgk_reverse_inc<LAT>(f, lam, d, imult, dimult, dg, p);
+  if constexpr (LAT == LAT_D2Q9_D2Q5) {
+    for (int i = 0; i < 9; ++i) d[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+  }
+  for (int i = 0; i < Q; ++i) li[i] = (double)lam[i] + (double)d[i];
+  *dgo = (double)dg;
+}
+
+template <class C>
+int dispatch_collide_inc(const lbm_config* c, const double* fin, double g, double* fout, double* sums) {
+  if (c->lattice == LBM_D2Q9 && c->collision == LBM_BGK) collide_inc<LAT_D2Q9, LBM_BGK, C>(c, fin, g, fout, sums);
+  else if (c->lattice == LBM_D2Q9) collide_inc<LAT_D2Q9, LBM_MRT, C>(c, fin, g, fout, sums);
+  else if (c->lattice == LBM_D3Q19 && c->collision == LBM_BGK) collide_inc<LAT_D3Q19, LBM_BGK, C>(c, fin, g, fout, sums);
+  else if (c->lattice == LBM_D3Q19) collide_inc<LAT_D3Q19, LBM_MRT, C>(c, fin, g, fout, sums);
+  else collide_inc<LAT_D2Q9_D2Q5, LBM_BGK, C>(c, fin, g, fout, sums);
+  return 0;
+}
+
+template <class C>
+int dispatch_reverse_inc(const lbm_config* c, const double* fin, double g, const double* lo,
+                         double* li, double* dg) {
+  if (c->collision != LBM_BGK) return -1;
+  if (c->lattice == LBM_D2Q9) reverse_inc<LAT_D2Q9, C>(c, fin, g, lo, li, dg);
+  else if (c->lattice == LBM_D3Q19) reverse_inc<LAT_D3Q19, C>(c, fin, g, lo, li, dg);
+  else reverse_inc<LAT_D2Q9_D2Q5, C>(c, fin, g, lo, li, dg);
+  return 0;
+}
+
 template <class C>
 int dispatch_collide(const lbm_config* c, const double* fin, double g, double* fout) {
   if (c->lattice == LBM_D2Q9 && c->collision == LBM_BGK) collide<LAT_D2Q9, LBM_BGK, C>(c, fin, g, fout);
@@ -119,6 +202,26 @@ int dispatch_reverse(const lbm_config* c, const double* fin, double g, const dou
 }  // namespace
 
 extern "C" {
+int dev_collide_inc(const lbm_config* c, int fp32, const double* fin, double g, double* fout,
+                    double* sums) {
+  return fp32 ? dispatch_collide_inc<float>(c, fin, g, fout, sums)
+              : dispatch_collide_inc<double>(c, fin, g, fout, sums);
+}
+int dev_reverse_inc(const lbm_config* c, int fp32, const double* fin, double g, const double* lo,
+                    double* li, double* dg) {
+  return fp32 ? dispatch_reverse_inc<float>(c, fin, g, lo, li, dg)
+              : dispatch_reverse_inc<double>(c, fin, g, lo, li, dg);
+}
+// Round<S>::apply(f, d) for n cells at one time step; out[i] is the stored value
+// (as double) of cell i.  half != 0 rounds to FP16.
+void dev_round(int half, float f, float d, int n, unsigned step, double* out) {
+  const unsigned key = step_key(step, kSaltForward);
+  for (int i = 0; i < n; ++i) {
+    Dither rnd((unsigned)i, key);
+    out[i] = half ? (double)__half2float(Round<__half>::apply(f, d, rnd))
+                  : (double)Round<float>::apply(f, d, rnd);
+  }
+}
 int dev_collide(const lbm_config* c, int fp32, const double* fin, double g, double* fout) {
   return fp32 ? dispatch_collide<float>(c, fin, g, fout) : dispatch_collide<double>(c, fin, g, fout);
 }

@@ -44,6 +44,10 @@ def devmath():
     dp = C.POINTER(C.c_double)
     lib.dev_collide.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp]
     lib.dev_reverse.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
+    lib.dev_collide_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp]
+    lib.dev_reverse_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
+    lib.dev_round.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
+    lib.dev_round.restype = None
     return lib
 
 
@@ -85,3 +89,88 @@ def test_device_operators_match_oracle(devmath, orc, name):
                                 li.ctypes.data_as(dp), dg.ctypes.data_as(dp))
             assert rel_inf(li, li_o) < tol * 10, (name, fp32, rel_inf(li, li_o))
             assert abs(dg[0] - dg_o) <= tol * 10 * max(abs(dg_o), np.abs(lo).max() * 1e-3), (name, fp32)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_increment_form_matches_oracle(devmath, orc, name):
+    """The FP32/FP16 storage path computes the collision (and, for BGK and the
+    thermal model, its transpose) as increments: f + d must be the same
+    operator (FP64 instantiation within 1e-14, FP32 within 5e-6)."""
+    cfg = CASES[name]
+    c = cfg.to_c()
+    dp = C.POINTER(C.c_double)
+    rng = np.random.default_rng(hash(name) % 2**32 + 1)
+    for _ in range(20):
+        fin, g, lo = _inputs(cfg, rng)
+        fo, _ = orc.collide_cell(cfg, fin, g)
+        li_o, dg_o = orc.reverse_cell(cfg, fin, g, lo)
+        for fp32, tol in ((0, 1e-14), (1, 5e-6)):
+            out = np.zeros(cfg.npop)
+            sums = np.zeros(5)
+            devmath.dev_collide_inc(C.byref(c), fp32, fin.ctypes.data_as(dp), g,
+                                    out.ctypes.data_as(dp), sums.ctypes.data_as(dp))
+            assert rel_inf(out, fo) < tol, (name, fp32, rel_inf(out, fo))
+            if cfg.collision != G.BGK:
+                continue
+            li = np.zeros(cfg.npop)
+            dg = np.zeros(1)
+            rc = devmath.dev_reverse_inc(C.byref(c), fp32, fin.ctypes.data_as(dp), g,
+                                         lo.ctypes.data_as(dp), li.ctypes.data_as(dp),
+                                         dg.ctypes.data_as(dp))
+            assert rc == 0
+            assert rel_inf(li, li_o) < tol * 10, (name, fp32, rel_inf(li, li_o))
+            assert abs(dg[0] - dg_o) <= tol * 10 * max(abs(dg_o), np.abs(lo).max() * 1e-3)
+
+
+@pytest.mark.parametrize("name", ["d2q9_bgk", "d2q9_mrt", "d3q19_bgk", "d3q19_mrt"])
+def test_increments_conserve_mass_and_momentum(devmath, orc, name):
+    """In a fluid cell (gamma = 1, no partial bounce-back) the FP32 increments
+    carry no mass and no momentum up to their own rounding: near equilibrium
+    |sum d| stays below 1e-6 of the largest increment, far below the rounding
+    of f itself that the plain form leaves in them."""
+    cfg = CASES[name]
+    c = cfg.to_c()
+    dp = C.POINTER(C.c_double)
+    rng = np.random.default_rng(7)
+    for _ in range(20):
+        fin, _, _ = _inputs(cfg, rng)
+        feq, _ = orc.collide_cell(cfg.replace(omega=1.0), fin, 1.0)   # the equilibrium of fin
+        fin = feq + 1e-4 * feq * rng.standard_normal(len(feq))        # small non-equilibrium part
+        out = np.zeros(cfg.npop)
+        sums = np.zeros(5)
+        devmath.dev_collide_inc(C.byref(c), 1, fin.ctypes.data_as(dp), 1.0,
+                                out.ctypes.data_as(dp), sums.ctypes.data_as(dp))
+        assert sums[4] > 0
+        assert np.abs(sums[:4]).max() < 1e-6 * sums[4], (name, sums)
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_stochastic_rounding_is_unbiased(devmath, half):
+    """Round<S>::apply(f, d) takes one of the two representable neighbours of
+    f + d, and over many cells its mean is f + d: round to nearest would be
+    off by the same fraction of a unit every time."""
+    n = 200000
+    out = np.zeros(n)
+    dp = C.POINTER(C.c_double)
+    dt = np.float16 if half else np.float32
+    for f, d in ((0.0123456, 3.1e-7), (-0.0071, 2.2e-6), (0.3, -1.3e-8)):
+        devmath.dev_round(half, f, d, n, 12345, out.ctypes.data_as(dp))
+        x = float(np.float32(f)) + float(np.float32(d))   # f and d as the kernel holds them
+        lo = float(dt(x))
+        if lo > x:
+            lo = float(np.nextafter(dt(x), dt(-np.inf)))
+        hi = float(np.nextafter(dt(lo), dt(np.inf)))
+        assert set(np.unique(out)) <= {lo, hi}, (f, d, np.unique(out)[:5])
+        ulp = hi - lo
+        assert abs(out.mean() - x) < 0.01 * ulp, (f, d, (out.mean() - x) / ulp)
+        rn_err = abs(float(dt(x)) - x) / ulp
+        assert rn_err > 0.05   # the cases are not trivially exact under round to nearest
+    # Within one unit of a power of two the noise, scaled to one binade, spans
+    # two or three neighbours; the mean stays within 0.25 units of the lower
+    # binade (such values are 1 in 2^23 of FP32 and 1 in 2^10 of FP16 ones).
+    for f, d in ((0.25, -1.3e-8), (0.5, -4e-9), (0.25, 1.3e-8)) if not half else \
+            ((0.25, -1e-4), (0.25, 3e-5), (0.5, -2e-4)):
+        devmath.dev_round(half, f, d, n, 999, out.ctypes.data_as(dp))
+        x = float(np.float32(f)) + float(np.float32(d))
+        ulp_lo = float(np.spacing(dt(min(abs(x), f) * 0.999)))
+        assert abs(out.mean() - x) < 0.25 * ulp_lo, (f, d, (out.mean() - x) / ulp_lo)
