@@ -328,7 +328,7 @@ def main():
     b_fwd = bytes_per_lu(G.STORE_FP32, "fwd") * cells
     ach_adj = b_adj / t_adj / 1e9
     ach_fwd = b_fwd / t_fwd / 1e9
-    traffic = None
+    traffic = traffic_fwd = None
     tr_path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if os.path.exists(tr_path):
         with open(tr_path) as f:
@@ -336,6 +336,8 @@ def main():
                 parts = ln.split()
                 if len(parts) == 2 and parts[0] == "k_adjoint_fp32_256x128x128":
                     traffic = int(parts[1])
+                if len(parts) == 2 and parts[0] == "k_forward_fp32_256x128x128":
+                    traffic_fwd = int(parts[1])
 
     # end to end through the C ABI with host buffers: design upload, full checkpointed
     # gradient (5000 steps, 64 device snapshots), sensitivity download
@@ -430,7 +432,8 @@ def main():
                      "traffic": traffic,
                      "forward": {"kernel": "k_forward<D3Q19,MRT,float>",
                                  "achieved": round(ach_fwd, 1), "frac": round(ach_fwd / peak, 4),
-                                 "bytes_per_lu": bytes_per_lu(G.STORE_FP32, "fwd")}},
+                                 "bytes_per_lu": bytes_per_lu(G.STORE_FP32, "fwd"),
+                                 "traffic": traffic_fwd}},
         "precision": {"fp32_vs_fp64_velocity_rel_l2_300_steps": errs.get("fp32"),
                       "fp16_vs_fp64_velocity_rel_l2_300_steps": errs.get("fp16"),
                       "fp64_mlups_fwd_adj": round(mlups64, 2),

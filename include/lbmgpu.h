@@ -214,6 +214,19 @@ int lbm_get_sensitivity(const lbm_handle* h, double* sens);
 int lbm_gradient(lbm_handle* h, int nsteps, int nsnapshots, double* J,
                  double* dJdgamma, lbm_gradient_stats* stats);
 
+/* Checkpoint schedules of lbm_gradient_schedule. */
+#define LBM_SCHEDULE_DYNAMIC 0 /* LBDynamicCheckpointing: online Wang placement */
+#define LBM_SCHEDULE_STATIC 1  /* LBStaticCheckpointing (topOpt/LBCheckpointing.cc:4-35,
+                                  staticCheckpointing.cc:3-63): the placement the online
+                                  schedule reaches after nsteps, planned before the sweep */
+
+/* lbm_gradient with the checkpoint schedule chosen: replaces the driver loop
+ * with LBStaticCheckpointing(nsnapshots, nsteps + 1, solver) as well
+ * (applications/pump2d/pump2d.cc:146, RobustPump2d/robustPump2d.cc:166).  The
+ * gradient does not depend on the schedule (recomputation is bit-exact). */
+int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnapshots, int schedule, double* J,
+                          double* dJdgamma, lbm_gradient_stats* stats);
+
 /* Device-time measurement for benchmarks: run `nsteps` forward steps
  * (which = 0), reverse steps over the current state (which = 1; the forward
  * state is left unchanged) or forward+reverse pairs (which = 2) on the
@@ -231,6 +244,12 @@ int lbm_autotune(lbm_handle* h, int nsteps);
 /* Block shape in use for the forward (which = 0) or reverse (which = 1) step. */
 int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by);
 
+/* Set the block shape of the forward (which = 0) or reverse (which = 1) step,
+ * e.g. one found by lbm_autotune in an earlier run: bx a multiple of 32,
+ * bx * by in {128, 256}.  No reference counterpart (the reference has no
+ * launch geometry). */
+int lbm_set_launch_shape(lbm_handle* h, int which, int bx, int by);
+
 /* Select the CUDA device (ordinal) that handles created afterwards by this
  * thread use (one process per GPU: the rank's local GPU). */
 int lbm_select_device(int ordinal);
@@ -242,6 +261,11 @@ int lbm_get_launch_count(const lbm_handle* h, int64_t* launches);
  * steps needed to reverse nsteps steps with nsnapshots slots
  * (WangCheckpointing.cc:72-162 with DynamicCheckpointing.cc:9-54). */
 int lbm_wang_recompute_count(int nsteps, int nsnapshots, int64_t* recomputed);
+
+/* Host-only: recomputed steps and states kept by the forward sweep (saved may
+ * be NULL) for a schedule, without a device. */
+int lbm_schedule_count(int nsteps, int nsnapshots, int schedule, int64_t* recomputed,
+                       int64_t* saved);
 
 /* ------------------------------------------------------------------------
  * Batches.  Up to LBM_MAX_BATCH lattices with the same lattice type, collision
@@ -272,6 +296,11 @@ int lbm_batch_forward(lbm_batch* b, int nsteps, double* J);
  * and dJdgamma (n pointers, entries may be NULL) may be NULL. */
 int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnapshots, int use_graph, double* J,
                        double* const* dJdgamma, lbm_gradient_stats* stats);
+
+/* lbm_batch_gradient with the checkpoint schedule chosen (LBM_SCHEDULE_*). */
+int lbm_batch_gradient_schedule(lbm_batch* b, int nsteps, int nsnapshots, int schedule,
+                                int use_graph, double* J, double* const* dJdgamma,
+                                lbm_gradient_stats* stats);
 /* As lbm_time_steps, for the batched kernels. */
 int lbm_batch_time_steps(lbm_batch* b, int which, int nsteps, float* ms);
 int lbm_batch_get_launch_count(const lbm_batch* b, int64_t* launches);

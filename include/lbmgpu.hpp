@@ -105,19 +105,44 @@ class AdjointLBSolver {
 
 // Forward sweep with Wang et al. dynamic checkpointing in device memory, the
 // reverse sweep, and dJ/dgamma: the driver loop of robustPump2d.cc:234-276
-// with LBDynamicCheckpointing as one call.
+// with LBDynamicCheckpointing (topOpt/LBCheckpointing.cc:37-65) as one call.
 class LBDynamicCheckpointing {
  public:
   LBDynamicCheckpointing(int numCheckpoints, IsothermalLBSolver& s) : k_(numCheckpoints), s_(s) {}
+  virtual ~LBDynamicCheckpointing() = default;
   int objectiveAndGradient(int numSteps, double* J, std::vector<double>* sens,
                            lbm_gradient_stats* stats = nullptr) {
     sens->resize((size_t)s_.numCells());
-    return lbm_gradient(s_.handle(), numSteps, k_, J, sens->data(), stats);
+    return lbm_gradient_schedule(s_.handle(), numSteps, k_, schedule(), J, sens->data(), stats);
   }
+
+ protected:
+  virtual int schedule() const { return LBM_SCHEDULE_DYNAMIC; }
 
  private:
   int k_;
   IsothermalLBSolver& s_;
+};
+
+// LBStaticCheckpointing(numCheckpoints, numTimesteps, solver)
+// (topOpt/LBCheckpointing.cc:4-35): placement planned before the sweep for
+// numTimesteps - 1 steps, as applications/pump2d/pump2d.cc:146 constructs it.
+class LBStaticCheckpointing : public LBDynamicCheckpointing {
+ public:
+  LBStaticCheckpointing(int numCheckpoints, int numTimesteps, IsothermalLBSolver& s)
+      : LBDynamicCheckpointing(numCheckpoints, s), nt_(numTimesteps) {}
+  // the reference plans for numTimesteps - 1 steps; other sweep lengths are refused
+  int objectiveAndGradient(int numSteps, double* J, std::vector<double>* sens,
+                           lbm_gradient_stats* stats = nullptr) {
+    if (numSteps != nt_ - 1) return LBM_ERR_ARG;
+    return LBDynamicCheckpointing::objectiveAndGradient(numSteps, J, sens, stats);
+  }
+
+ protected:
+  int schedule() const override { return LBM_SCHEDULE_STATIC; }
+
+ private:
+  int nt_;
 };
 
 }  // namespace lbmgpu

@@ -791,9 +791,16 @@ int lbm_get_sensitivity(const lbm_handle* hc, double* sens) {
 
 int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgamma,
                  lbm_gradient_stats* stats) {
+  return lbm_gradient_schedule(h, nsteps, nsnap, LBM_SCHEDULE_DYNAMIC, J, dJdgamma, stats);
+}
+
+int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, double* J,
+                          double* dJdgamma, lbm_gradient_stats* stats) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
   if (nsteps < 1) return fail(h, LBM_ERR_ARG, "nsteps %d < 1", nsteps);
   if (nsnap < 2) return fail(h, LBM_ERR_ARG, "nsnapshots %d < 2", nsnap);
+  if (schedule != LBM_SCHEDULE_DYNAMIC && schedule != LBM_SCHEDULE_STATIC)
+    return fail(h, LBM_ERR_ARG, "unknown checkpoint schedule %d", schedule);
   if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
   int rc;
   // snapshot slots in device memory
@@ -816,6 +823,9 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
   const bool obj = h->cfg.objective != LBM_OBJ_NONE;
   const size_t sb = state_bytes(h);
   WangSchedule ws(nsnap);
+  const bool planned = schedule == LBM_SCHEDULE_STATIC;
+  if (planned) ws.plan_static(nsteps);
+  auto place = [&](int index) { return planned ? ws.make_checkpoint_static(index) : ws.make_checkpoint(index); };
   // Checkpoints without copies: every state lives in one of the pool's K+2
   // buffers and saves/restores only move labels (StatePool).
   StatePool pool;
@@ -828,6 +838,7 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
     return r;
   };
   auto save = [&](int slot) -> int {
+    if (slot < 0) return 0;   // a state the static plan does not keep
     const int dst = pool.save(slot);
     if (dst >= 0)
       CUDA_OR_FAIL(h, cudaMemcpyAsync(pool_buffer(h, dst), cur_buf(), sb, cudaMemcpyDeviceToDevice,
@@ -851,10 +862,13 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
   }
   // J = sum_t F(f_t), summed in the block partials across the sweep
   if (obj && (rc = begin_accumulate(h))) return rc;
-  if ((rc = save(ws.make_checkpoint(0)))) return rc;
+  if ((rc = save(place(0)))) {
+    h->accumulate = false;
+    return rc;
+  }
   for (int s = 0; s < nsteps; ++s) {
     if ((rc = advance((obj && s >= 1) ? h->jdev : nullptr))) break;
-    if ((rc = save(ws.make_checkpoint(s + 1)))) break;
+    if ((rc = save(place(s + 1)))) break;
   }
   if (!rc && obj && !(rc = objective_at(h, cur_buf(), h->jdev))) rc = end_accumulate(h, h->jdev);
   h->accumulate = false;
@@ -980,6 +994,17 @@ int lbm_autotune(lbm_handle* h, int nsteps) {
   return rc;
 }
 
+int lbm_set_launch_shape(lbm_handle* h, int which, int bx, int by) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (which < 0 || which > 1) return fail(h, LBM_ERR_ARG, "which must be 0 (forward) or 1 (reverse)");
+  if (bx < 32 || bx % 32 != 0 || by < 1 || (bx * by != 128 && bx * by != 256))
+    return fail(h, LBM_ERR_ARG, "block %dx%d: bx must be a multiple of 32 and bx*by 128 or 256", bx, by);
+  Geometry g = make_geometry(h->cfg.nx, h->cfg.ny, h->cfg.nz, bx, by);
+  if (g.nblocks > h->partial_cap) return fail(h, LBM_ERR_ARG, "block %dx%d gives too many blocks", bx, by);
+  (which == 0 ? h->geo_fwd : h->geo_adj) = g;
+  return LBM_OK;
+}
+
 int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by) {
   if (!h || !bx || !by || which < 0 || which > 1) return fail(nullptr, LBM_ERR_ARG, "bad arguments");
   const Geometry& g = which == 0 ? h->geo_fwd : h->geo_adj;
@@ -1005,12 +1030,28 @@ int lbm_get_launch_count(const lbm_handle* h, int64_t* n) {
 }
 
 int lbm_wang_recompute_count(int nsteps, int nsnap, int64_t* recomputed) {
+  return lbm_schedule_count(nsteps, nsnap, LBM_SCHEDULE_DYNAMIC, recomputed, nullptr);
+}
+
+int lbm_schedule_count(int nsteps, int nsnap, int schedule, int64_t* recomputed, int64_t* saved) {
   if (!recomputed || nsteps < 1 || nsnap < 2)
     return fail(nullptr, LBM_ERR_ARG, "need nsteps >= 1, nsnapshots >= 2");
+  if (schedule != LBM_SCHEDULE_DYNAMIC && schedule != LBM_SCHEDULE_STATIC)
+    return fail(nullptr, LBM_ERR_ARG, "unknown checkpoint schedule %d", schedule);
   WangSchedule ws(nsnap);
+  const bool planned = schedule == LBM_SCHEDULE_STATIC;
+  if (planned) ws.plan_static(nsteps);
   std::vector<int> slot_step(nsnap, -1);
   int state = 0;
-  for (int s = 0; s <= nsteps; ++s) slot_step[ws.make_checkpoint(s)] = s;
+  int64_t kept = 0;
+  for (int s = 0; s <= nsteps; ++s) {
+    const int slot = planned ? ws.make_checkpoint_static(s) : ws.make_checkpoint(s);
+    if (slot >= 0) {
+      slot_step[slot] = s;
+      ++kept;
+    }
+  }
+  if (saved) *saved = kept;
   WangSchedule::Actions act;
   act.advance = [&]() { ++state; return 0; };
   act.restore = [&](int step, int slot) {
@@ -1068,7 +1109,7 @@ struct lbm_batch {
   int nsm = 1;
   int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
   cudaGraphExec_t graph = nullptr;
-  int graph_steps = -1, graph_snap = -1;
+  int graph_steps = -1, graph_snap = -1, graph_schedule = -1;
   int64_t graph_recomputed = 0;
   int64_t graph_launches = 0;            // kernels in the captured sequence
   int end_cur[LBM_MAX_BATCH] = {}, end_lcur[LBM_MAX_BATCH] = {};   // host state after it
@@ -1232,13 +1273,16 @@ int batch_init(lbm_batch* b, int buf) {
 // The checkpointed forward + reverse sequence of lbm_batch_gradient, issued on
 // the batch stream (and so capturable as one graph).  All lattices follow one
 // schedule, so one StatePool labels the buffers of every lattice alike.
-int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
+int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int schedule, int64_t* recomputed) {
   int rc;
   for (int i = 0; i < b->n; ++i) {
     b->h[i]->cur = 0;
     b->h[i]->lcur = 0;
   }
   WangSchedule ws(nsnap);
+  const bool planned = schedule == LBM_SCHEDULE_STATIC;
+  if (planned) ws.plan_static(nsteps);
+  auto place = [&](int index) { return planned ? ws.make_checkpoint_static(index) : ws.make_checkpoint(index); };
   StatePool pool;
   pool.reset(nsnap, 0);
   double* res[LBM_MAX_BATCH];
@@ -1249,6 +1293,7 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
     return r;
   };
   auto save = [&](int slot) -> int {
+    if (slot < 0) return 0;   // a state the static plan does not keep
     const int dst = pool.save(slot);
     return dst >= 0 ? batch_copy(b, pool.current(), dst) : 0;
   };
@@ -1264,13 +1309,13 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
   auto stop_accumulating = [&]() {
     for (int i = 0; i < b->n; ++i) b->h[i]->accumulate = false;
   };
-  if ((rc = save(ws.make_checkpoint(0)))) {
+  if ((rc = save(place(0)))) {
     stop_accumulating();
     return rc;
   }
   for (int s = 0; s < nsteps; ++s) {
     for (int i = 0; i < b->n; ++i) res[i] = s >= 1 ? b->h[i]->jdev : nullptr;
-    if ((rc = advance(res)) || (rc = save(ws.make_checkpoint(s + 1)))) {
+    if ((rc = advance(res)) || (rc = save(place(s + 1)))) {
       stop_accumulating();
       return rc;
     }
@@ -1317,7 +1362,7 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int64_t* recomputed) {
 void batch_destroy_graph(lbm_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
-  b->graph_steps = b->graph_snap = -1;
+  b->graph_steps = b->graph_snap = b->graph_schedule = -1;
 }
 
 }  // namespace
@@ -1482,8 +1527,16 @@ int lbm_batch_forward(lbm_batch* b, int nsteps, double* J) {
 
 int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, double* J,
                        double* const* dJdgamma, lbm_gradient_stats* stats) {
+  return lbm_batch_gradient_schedule(b, nsteps, nsnap, LBM_SCHEDULE_DYNAMIC, use_graph, J,
+                                     dJdgamma, stats);
+}
+
+int lbm_batch_gradient_schedule(lbm_batch* b, int nsteps, int nsnap, int schedule, int use_graph,
+                                double* J, double* const* dJdgamma, lbm_gradient_stats* stats) {
   if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
   if (nsteps < 1 || nsnap < 2) return bfail(b, LBM_ERR_ARG, "need nsteps >= 1 and nsnapshots >= 2");
+  if (schedule != LBM_SCHEDULE_DYNAMIC && schedule != LBM_SCHEDULE_STATIC)
+    return bfail(b, LBM_ERR_ARG, "unknown checkpoint schedule %d", schedule);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     if (!h->have_design) return bfail(b, LBM_ERR_STATE, "lattice %d has no design", i);
@@ -1507,12 +1560,13 @@ int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, doubl
   int64_t recomputed = 0;
   cudaEventRecord(b->ev[0], b->stream);
   if (use_graph) {
-    if (!(b->graph && b->graph_steps == nsteps && b->graph_snap == nsnap)) {
+    if (!(b->graph && b->graph_steps == nsteps && b->graph_snap == nsnap &&
+          b->graph_schedule == schedule)) {
       batch_destroy_graph(b);
       cudaGraph_t g = nullptr;
       const int64_t l0 = b->launches;
       BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      rc = batch_sequence(b, nsteps, nsnap, &recomputed);
+      rc = batch_sequence(b, nsteps, nsnap, schedule, &recomputed);
       b->graph_launches = b->launches - l0;
       cudaError_t e = cudaStreamEndCapture(b->stream, &g);
       if (rc) {
@@ -1528,6 +1582,7 @@ int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, doubl
       }
       b->graph_steps = nsteps;
       b->graph_snap = nsnap;
+      b->graph_schedule = schedule;
       b->graph_recomputed = recomputed;
       for (int i = 0; i < b->n; ++i) {
         b->end_cur[i] = b->h[i]->cur;
@@ -1550,7 +1605,7 @@ int lbm_batch_gradient(lbm_batch* b, int nsteps, int nsnap, int use_graph, doubl
       h->have_state = h->have_adjoint = true;
     }
   } else {
-    if ((rc = batch_sequence(b, nsteps, nsnap, &recomputed))) return rc;
+    if ((rc = batch_sequence(b, nsteps, nsnap, schedule, &recomputed))) return rc;
   }
   cudaEventRecord(b->ev[1], b->stream);
   BCUDA(b, cudaStreamSynchronize(b->stream));

@@ -48,6 +48,31 @@ class WangSchedule {
 
   int64_t recomputed() const { return recomputed_; }
 
+  // Static placement (StaticCheckpointing, topOpt/staticCheckpointing.cc:3-63):
+  // the checkpoints this schedule computes for `nsteps` steps from an empty
+  // list, oldest first; after plan_static, make_checkpoint_static keeps exactly
+  // those states and the reverse sweep (get_forward_solution) is unchanged.
+  void plan_static(int nsteps) {
+    reset();
+    compute_new_checkpoints(nsteps);
+    plan_.clear();
+    int tail = head_;
+    while (tail >= 0 && nodes_[tail].next >= 0) tail = nodes_[tail].next;
+    for (int id = tail; id >= 0; id = nodes_[id].prev) plan_.push_back({nodes_[id].step, nodes_[id].level});
+    reset();
+    plan_pos_ = 0;
+  }
+
+  // Static counterpart of make_checkpoint: the slot to copy state `index`
+  // into, or -1 when the plan does not keep it.
+  int make_checkpoint_static(int index) {
+    if (plan_pos_ >= plan_.size() || plan_[plan_pos_].step != index) return -1;
+    const int slot = pop_avail();
+    push_front(index, plan_[plan_pos_].level, slot);
+    ++plan_pos_;
+    return slot;
+  }
+
   // Place checkpoint `index`; returns the slot the caller must copy the state into.
   int make_checkpoint(int index) {
     if (head_ < 0) {
@@ -169,6 +194,12 @@ class WangSchedule {
     }
     return start;
   }
+
+  struct Planned {
+    int step, level;
+  };
+  std::vector<Planned> plan_;
+  size_t plan_pos_ = 0;
 
   int nslots_;
   std::vector<Node> nodes_;

@@ -38,6 +38,7 @@ BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE = 1, 2, 3
 FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
 PROFILE_UNIFORM, PROFILE_PARABOLIC = 0, 1
 OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX, OBJ_OUTFLOW = 0, 1, 2, 3, 4
+SCHEDULE_DYNAMIC, SCHEDULE_STATIC = 0, 1
 MAX_BC = 8
 
 STATUS_TEXT = {0: "ok", -1: "bad argument", -2: "unsupported", -3: "CUDA error",
@@ -207,7 +208,14 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_batch_get_launch_count": (C.c_int, [H, C.POINTER(C.c_int64)]),
         "lbm_autotune": (C.c_int, [H, C.c_int]),
         "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
         "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
+        "lbm_schedule_count": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int64)]),
+        "lbm_gradient_schedule": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp, dp,
+                                            C.POINTER(CGradStats)]),
+        "lbm_batch_gradient_schedule": (C.c_int, [H, C.c_int, C.c_int, C.c_int, C.c_int, dp,
+                                                  C.POINTER(dp), C.POINTER(CGradStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -230,6 +238,17 @@ def select_device(ordinal: int) -> None:
     rc = lib.lbm_select_device(int(ordinal))
     if rc:
         raise LBMError(rc, lib.lbm_last_error(None).decode())
+
+
+def schedule_count(nsteps: int, nsnapshots: int, schedule: int = SCHEDULE_DYNAMIC):
+    """(recomputed steps, states kept by the forward sweep) of a checkpoint schedule."""
+    lib = load_library()
+    rec, saved = C.c_int64(), C.c_int64()
+    rc = lib.lbm_schedule_count(int(nsteps), int(nsnapshots), int(schedule), C.byref(rec),
+                                C.byref(saved))
+    if rc:
+        raise LBMError(rc, lib.lbm_last_error(None).decode())
+    return rec.value, saved.value
 
 
 def wang_recompute_count(nsteps: int, nsnapshots: int) -> int:
@@ -330,12 +349,12 @@ class Handle:
         self._check(self.lib.lbm_get_sensitivity(self.h, _ptr(s)))
         return s
 
-    def gradient(self, nsteps: int, nsnapshots: int):
+    def gradient(self, nsteps: int, nsnapshots: int, schedule: int = SCHEDULE_DYNAMIC):
         J = np.zeros(1)
         s = np.empty(self.cfg.ncells)
         st = CGradStats()
-        self._check(self.lib.lbm_gradient(self.h, int(nsteps), int(nsnapshots), _ptr(J),
-                                          _ptr(s), C.byref(st)))
+        self._check(self.lib.lbm_gradient_schedule(self.h, int(nsteps), int(nsnapshots),
+                                                   int(schedule), _ptr(J), _ptr(s), C.byref(st)))
         return float(J[0]), s, st
 
     def time_steps(self, which: int, nsteps: int) -> float:
@@ -352,6 +371,9 @@ class Handle:
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_get_launch_shape(self.h, int(which), C.byref(bx), C.byref(by)))
         return bx.value, by.value
+
+    def set_launch_shape(self, which: int, bx: int, by: int):
+        self._check(self.lib.lbm_set_launch_shape(self.h, int(which), int(bx), int(by)))
 
     def launch_count(self) -> int:
         n = C.c_int64()
@@ -428,13 +450,15 @@ class Batch:
         self._check(self.lib.lbm_batch_forward(self.b, int(nsteps), _ptr(J)))
         return J
 
-    def gradient(self, nsteps: int, nsnapshots: int, use_graph: bool = True):
+    def gradient(self, nsteps: int, nsnapshots: int, use_graph: bool = True,
+                 schedule: int = SCHEDULE_DYNAMIC):
         J = np.zeros(len(self))
         sens = [np.empty(c.ncells) for c in self.cfgs]
         ptrs = (C.POINTER(C.c_double) * len(self))(*[_ptr(a) for a in sens])
         st = CGradStats()
-        self._check(self.lib.lbm_batch_gradient(self.b, int(nsteps), int(nsnapshots),
-                                                int(bool(use_graph)), _ptr(J), ptrs, C.byref(st)))
+        self._check(self.lib.lbm_batch_gradient_schedule(
+            self.b, int(nsteps), int(nsnapshots), int(schedule), int(bool(use_graph)), _ptr(J),
+            ptrs, C.byref(st)))
         return J, sens, st
 
     def time_steps(self, which: int, nsteps: int) -> float:
@@ -493,11 +517,20 @@ class AdjointLBSolver:
 
 class LBDynamicCheckpointing:
     """Checkpointed forward+adjoint with Wang et al. dynamic checkpointing
-    (topOpt/LBCheckpointing.cc:322-351) and nsnapshots device slots."""
+    (topOpt/LBCheckpointing.cc:37-65) and nsnapshots device slots."""
+
+    schedule = SCHEDULE_DYNAMIC
 
     def __init__(self, nsnapshots: int, solver: IsothermalLBSolver):
         self.k = int(nsnapshots)
         self.solver = solver
 
     def gradient(self, nsteps: int):
-        return self.solver.handle.gradient(nsteps, self.k)
+        return self.solver.handle.gradient(nsteps, self.k, self.schedule)
+
+
+class LBStaticCheckpointing(LBDynamicCheckpointing):
+    """LBStaticCheckpointing (topOpt/LBCheckpointing.cc:4-35): the checkpoint
+    placement is planned before the forward sweep; same gradient."""
+
+    schedule = SCHEDULE_STATIC

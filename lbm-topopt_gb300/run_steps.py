@@ -45,12 +45,18 @@ def main():
     ap.add_argument("--fwd", type=int, default=10)
     ap.add_argument("--adj", type=int, default=10)
     ap.add_argument("--autotune", action="store_true", help="pick block shapes first")
+    ap.add_argument("--shape", type=int, nargs=4, default=None, metavar=("FBX", "FBY", "ABX", "ABY"),
+                    help="fixed block shapes of the forward and reverse steps (reproducible "
+                         "profiles: the autotuner's choice can change under a profiler)")
     a = ap.parse_args()
     cfg, gamma, _ = build_workload(a.workload, STORAGE[a.storage], a.size)
     with G.Handle(cfg) as h:
         h.set_design(gamma)
         h.init_equilibrium()
-        if a.autotune:
+        if a.shape:
+            h.set_launch_shape(0, a.shape[0], a.shape[1])
+            h.set_launch_shape(1, a.shape[2], a.shape[3])
+        elif a.autotune:
             print("block shapes (forward, reverse):", h.autotune())
         ms_f = h.time_steps(0, a.fwd) if a.fwd > 0 else 0.0
         ms_a = h.time_steps(1, a.adj) if a.adj > 0 else 0.0

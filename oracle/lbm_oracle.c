@@ -1537,6 +1537,62 @@ int orc_wang_count(int nsteps, int nsnap, int64_t* recomputed, int* ok_out) {
   return 0;
 }
 
+/* StaticCheckpointing (topOpt/staticCheckpointing.cc:3-63): the placement the
+ * online schedule computes for `nsteps` steps from an empty list
+ * (computeNewCheckpoints(numTimestep - 1) with numTimestep = nsteps + 1),
+ * recorded oldest first; the forward sweep then saves exactly those states and
+ * the reverse sweep is the dynamic one.  *saved = states kept by the sweep. */
+int orc_static_count(int nsteps, int nsnap, int64_t* recomputed, int* ok_out, int* saved) {
+  if (nsnap < 2 || nsteps < 1) return -1;
+  wang_t w;
+  int cap = 4 * (nsteps + nsnap) + 16;
+  int* plan_step = (int*)calloc(nsnap + 1, sizeof(int));
+  int* plan_level = (int*)calloc(nsnap + 1, sizeof(int));
+  memset(&w, 0, sizeof(w));
+  w.cap = cap;
+  w.n = (wnode*)calloc(cap, sizeof(wnode));
+  w.freeq = (int*)calloc(cap, sizeof(int));
+  w.avail = (int*)calloc(nsnap, sizeof(int));
+  w.slot_state = (int*)calloc(nsnap, sizeof(int));
+  if (!w.n || !w.freeq || !w.avail || !w.slot_state || !plan_step || !plan_level) return -4;
+  w.head = -1;
+  for (int i = 0; i < nsnap; ++i) w.avail[w.navail++] = i;
+  wang_compute_new(&w, nsteps);
+  /* the list from the back (oldest) to the front */
+  int nplan = 0, tail = w.head;
+  while (tail >= 0 && w.n[tail].next >= 0) tail = w.n[tail].next;
+  for (int id = tail; id >= 0 && nplan <= nsnap; id = w.n[id].prev) {
+    plan_step[nplan] = w.n[id].step;
+    plan_level[nplan] = w.n[id].level;
+    ++nplan;
+  }
+  /* reset: an empty list and all slots free again */
+  memset(w.n, 0, cap * sizeof(wnode));
+  w.head = -1;
+  w.nused = 0;
+  w.fq_head = w.fq_tail = w.fq_len = 0;
+  w.navail = 0;
+  for (int i = 0; i < nsnap; ++i) w.avail[w.navail++] = i;
+  w.recomputed = 0;
+  int pos = 0;
+  for (int s = 0; s <= nsteps; ++s) {
+    if (pos < nplan && plan_step[pos] == s) {
+      int slot = w.avail[--w.navail];
+      wpush_front(&w, s, plan_level[pos], slot);
+      w.slot_state[slot] = s;
+      ++pos;
+    }
+  }
+  if (saved) *saved = pos;
+  int ok = 1;
+  for (int s = nsteps; s >= 1; --s) wang_get(&w, s, &ok);
+  *recomputed = w.recomputed;
+  if (ok_out) *ok_out = ok;
+  free(w.n); free(w.freeq); free(w.avail); free(w.slot_state);
+  free(plan_step); free(plan_level);
+  return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* CPU baseline timing: wall time of nsteps forward steps and of nsteps reverse
  * steps of this restatement on nthreads host threads (0 = all). */

@@ -38,6 +38,7 @@ int orc_reverse_cell(const lbm_config* cfg, const double* fin, double gamma,
                      const double* lam_out, double* lam_in, double* dgamma);
 int orc_objective(const lbm_config* cfg, const double* f, const double* gamma, double* J);
 int orc_wang_count(int nsteps, int nsnap, int64_t* recomputed, int* ok);
+int orc_static_count(int nsteps, int nsnap, int64_t* recomputed, int* ok, int* saved);
 /* Wall time of nsteps forward and nsteps reverse steps on nthreads threads (0 = all). */
 int orc_time_steps(const lbm_config* cfg, const double* gamma, int nsteps, int nthreads,
                    double* sec_fwd, double* sec_adj);

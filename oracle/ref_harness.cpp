@@ -34,6 +34,7 @@
 #include "dynamics/MRT3d.hh"
 #include "adjointDynamics/reverseMRT3d.hh"
 #include "topOpt/dynamicCheckpointing.hh"
+#include "topOpt/staticCheckpointing.hh"
 
 #include "../include/lbmgpu.h"
 
@@ -521,6 +522,30 @@ class CountingCheckpointing : public DynamicCheckpointing {
   }
 };
 
+/* The reference's static placement, driven the same way. */
+class CountingStatic : public StaticCheckpointing {
+ public:
+  CountingStatic(PetscInt k, PetscInt nt, Vec v) : StaticCheckpointing(k, nt, v) {}
+  size_t numSaved() const { return checkpoints.size(); }
+  double state = 0.;
+  long long recomputed = 0;
+
+ protected:
+  PetscErrorCode advance(void*) override {
+    state += 1.;
+    ++recomputed;
+    return 0;
+  }
+  PetscErrorCode setSolverState(PetscInt, Vec v, void*) override {
+    state = v->v[0];
+    return 0;
+  }
+  PetscErrorCode copyFromSolverState(Vec v, void*) override {
+    v->v[0] = state;
+    return 0;
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -611,6 +636,31 @@ int ref_wang_count(int nsteps, int nsnap, long long* recomputed, int* ok) {
     cur.v[0] = s;
     ck.makeCheckpoint(s, &cur, nullptr);
   }
+  int good = 1;
+  for (int s = nsteps; s >= 1; --s) {
+    ck.getForwardSolution(s, &cur, nullptr);
+    if (cur.v[0] != (double)s) good = 0;
+  }
+  *recomputed = ck.recomputed;
+  if (ok) *ok = good;
+  return 0;
+}
+
+/* StaticCheckpointing(nsnap, nsteps + 1): the forward sweep offers states
+ * 0..nsteps (as the applications do, e.g. pump2d.cc:146); saved counts the
+ * states it kept. */
+int ref_static_count(int nsteps, int nsnap, long long* recomputed, int* ok, int* saved) {
+  if (nsnap < 2 || nsteps < 1) return -1;
+  _p_Vec proto;
+  proto.v.assign(1, 0.);
+  CountingStatic ck(nsnap, nsteps + 1, &proto);
+  _p_Vec cur;
+  cur.v.assign(1, 0.);
+  for (int s = 0; s <= nsteps; ++s) {
+    cur.v[0] = s;
+    ck.makeCheckpoint(s, &cur, nullptr);
+  }
+  if (saved) *saved = (int)ck.numSaved();
   int good = 1;
   for (int s = nsteps; s >= 1; --s) {
     ck.getForwardSolution(s, &cur, nullptr);

@@ -66,6 +66,17 @@ inline PetscErrorCode PetscObjectGetComm(PetscObject, MPI_Comm* c) {
   *c = 0;
   return 0;
 }
+template <class T>
+inline PetscErrorCode PetscMalloc1(PetscInt n, T** p) {
+  *p = new T[n > 0 ? n : 1];
+  return 0;
+}
+template <class T>
+inline PetscErrorCode PetscFree(T*& p) {
+  delete[] p;
+  p = nullptr;
+  return 0;
+}
 inline PetscErrorCode VecCopy(Vec a, Vec b) {
   b->v = a->v;
   return 0;

@@ -68,7 +68,19 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "gradient: %s\n", solver.lastError().c_str());
     return 1;
   }
+  // the same with the static placement, constructed as applications/pump2d/pump2d.cc:146
+  lbmgpu::LBStaticCheckpointing scheck(8, nsteps + 1, solver);
+  double Js = 0.;
+  std::vector<double> ssens;
+  lbm_gradient_stats sst;
+  if ((ierr = scheck.objectiveAndGradient(nsteps, &Js, &ssens, &sst))) {
+    std::fprintf(stderr, "static gradient: %s\n", solver.lastError().c_str());
+    return 1;
+  }
+  const bool same = Js == Jg && ssens == sens;
   std::printf("J %.17g\nJgrad %.17g\nrecomputed %lld\n", J, Jg, (long long)st.recomputed_steps);
+  std::printf("static_same %d\nstatic_recomputed %lld\n", same ? 1 : 0,
+              (long long)sst.recomputed_steps);
   std::printf("sens");
   for (double s : sens) std::printf(" %.17g", s);
   std::printf("\nf");

@@ -71,6 +71,15 @@ def main():
     np.savetxt(os.path.join(HERE, "wang_schedule.txt"), np.array(table, dtype=np.int64), fmt="%d",
                header="nsteps nsnapshots recomputed_steps reversal_exact (reference WangCheckpointing + DynamicCheckpointing)")
     print("wang table", len(table))
+    table = []
+    for N in (1, 2, 3, 10, 50, 100, 777, 1000, 2000, 4000, 5000, 10000, 20000):
+        for K in (2, 3, 7, 16, 20, 64):
+            r, ok, saved = ref.static_count(N, K)
+            table.append((N, K, r, int(ok), saved))
+    np.savetxt(os.path.join(HERE, "static_schedule.txt"), np.array(table, dtype=np.int64), fmt="%d",
+               header="nsteps nsnapshots recomputed_steps reversal_exact saved_states "
+                      "(reference StaticCheckpointing(K, nsteps + 1) + WangCheckpointing)")
+    print("static table", len(table))
 
 
 if __name__ == "__main__":

@@ -37,6 +37,9 @@ def _bind(lib, prefix):
     if prefix == "orc_":
         lib.orc_wang_count.restype = C.c_int
         lib.orc_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+        lib.orc_static_count.restype = C.c_int
+        lib.orc_static_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int)]
         lib.orc_forward_from.restype = C.c_int
         lib.orc_forward_from.argtypes = [cp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
         lib.orc_init.restype = C.c_int
@@ -49,6 +52,9 @@ def _bind(lib, prefix):
         lib.ref_wang_count.restype = C.c_int
         lib.ref_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_longlong),
                                        C.POINTER(C.c_int)]
+        lib.ref_static_count.restype = C.c_int
+        lib.ref_static_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int)]
     return lib
 
 
@@ -130,6 +136,16 @@ class Checker:
         if rc:
             raise RuntimeError("wang_count failed: %d" % rc)
         return int(r.value), bool(ok.value)
+
+    def static_count(self, nsteps, nsnap):
+        """StaticCheckpointing(nsnap, nsteps + 1): (recomputed, reversal exact, states kept)."""
+        r = C.c_int64() if self.prefix == "orc_" else C.c_longlong()
+        ok, saved = C.c_int(), C.c_int()
+        rc = self._fn("static_count")(int(nsteps), int(nsnap), C.byref(r), C.byref(ok),
+                                      C.byref(saved))
+        if rc:
+            raise RuntimeError("static_count failed: %d" % rc)
+        return int(r.value), bool(ok.value), int(saved.value)
 
 
 def oracle() -> Checker:

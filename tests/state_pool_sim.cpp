@@ -5,7 +5,7 @@
 // state of step t, that no time step writes over its own input or a live
 // checkpoint, and counts the copies the pool asked for.
 //
-//   state_pool_sim NSTEPS NSNAP   -> prints "ok <copies> <recomputed>" or "FAIL ..."
+//   state_pool_sim NSTEPS NSNAP [static] -> prints "ok <copies> <recomputed>" or "FAIL ..."
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
@@ -18,13 +18,16 @@ using lbm::StatePool;
 using lbm::WangSchedule;
 
 int main(int argc, char** argv) {
-  if (argc != 3) return 2;
+  if (argc != 3 && argc != 4) return 2;
   const int nsteps = std::atoi(argv[1]), nsnap = std::atoi(argv[2]);
+  const bool planned = argc == 4;
   std::vector<int> content(nsnap + 2, -100);   // buffer -> step held
   std::vector<int> slot_step(nsnap, -1);       // slot -> checkpointed step
   StatePool pool;
   pool.reset(nsnap, 0);
   WangSchedule ws(nsnap);
+  if (planned) ws.plan_static(nsteps);
+  auto place = [&](int index) { return planned ? ws.make_checkpoint_static(index) : ws.make_checkpoint(index); };
   long copies = 0;
   int t = 0;
   char err[256] = {0};
@@ -44,6 +47,7 @@ int main(int argc, char** argv) {
     ++t;
   };
   auto save = [&](int slot) {
+    if (slot < 0) return;   // not kept by the static plan
     const int dst = pool.save(slot);
     if (dst >= 0) {
       ++copies;
@@ -58,10 +62,10 @@ int main(int argc, char** argv) {
       content[out] = 0;
       pool.set_current(out);
     }
-    save(ws.make_checkpoint(0));
+    save(place(0));
     for (int s = 0; s < nsteps; ++s) {
       advance();
-      save(ws.make_checkpoint(s + 1));
+      save(place(s + 1));
     }
     WangSchedule::Actions act;
     act.advance = [&]() {

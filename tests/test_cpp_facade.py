@@ -56,3 +56,6 @@ def test_cpp_driver_matches_oracle(driver, orc):
     assert rel_inf(f, fo) < 1e-12
     assert rel_inf(sens, so) < 1e-12
     assert int(lines["recomputed"][0]) == G.wang_recompute_count(n, 8)
+    # LBStaticCheckpointing: same gradient bit for bit, the reference's recompute count
+    assert lines["static_same"][0] == "1"
+    assert int(lines["static_recomputed"][0]) == orc.static_count(n, 8)[0]

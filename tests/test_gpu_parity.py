@@ -259,3 +259,52 @@ def test_errors_are_reported():
     with pytest.raises(G.LBMError) as e:
         G.Handle(bad)
     assert e.value.code == -1
+
+
+@pytest.mark.parametrize("storage", [G.STORE_FP64, G.STORE_FP32])
+def test_launch_shape_does_not_change_results(storage):
+    """Every block shape gives the same populations bit for bit (the FP32
+    rounding noise is keyed on the cell, not the block); an invalid shape is
+    refused."""
+    cfg = W.duct_3d(40, 12, 10, nsteps=30).replace(storage=storage)
+    gamma = W.design_3d(40, 12, 10, 5)
+    out = []
+    for shape in ((128, 2), (32, 4), (64, 2)):
+        with G.Handle(cfg) as h:
+            h.set_launch_shape(0, *shape)
+            h.set_launch_shape(1, *shape)
+            assert h.launch_shape(0) == shape and h.launch_shape(1) == shape
+            h.set_design(gamma)
+            h.init_equilibrium()
+            J = h.forward(30)
+            out.append((h.populations(), J))
+    for f, J in out[1:]:
+        assert np.array_equal(f, out[0][0])
+        assert abs(J - out[0][1]) <= 1e-13 * abs(out[0][1])
+    with G.Handle(cfg) as h:
+        for bad in ((48, 4), (32, 3), (16, 8)):
+            with pytest.raises(G.LBMError) as e:
+                h.set_launch_shape(0, *bad)
+            assert e.value.code == -1
+
+
+def test_static_schedule_gives_the_same_gradient(orc):
+    """LBStaticCheckpointing and LBDynamicCheckpointing: the same dJ/dgamma bit
+    for bit (recomputation is exact) and the reference's recompute counts."""
+    n, k = 90, 6
+    cfg = W.channel_2d(30, 14, nsteps=n, amp=0.1, period=40.0)
+    gamma = W.design_2d(30, 14, 17)
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        Jd, sd, std = h.gradient(n, k, G.SCHEDULE_DYNAMIC)
+        Js, ss, sts = h.gradient(n, k, G.SCHEDULE_STATIC)
+    assert Js == Jd and np.array_equal(ss, sd)
+    assert sts.recomputed_steps == orc.static_count(n, k)[0]
+    assert std.recomputed_steps == orc.wang_count(n, k)[0]
+    insts = [(cfg, gamma), (W.channel_2d(20, 10, nsteps=n), W.design_2d(20, 10, 18))]
+    with G.Batch([c for c, _ in insts]) as b:
+        for i, (_, g) in enumerate(insts):
+            b[i].set_design(g)
+        Jb, sb, _ = b.gradient(n, k, use_graph=True, schedule=G.SCHEDULE_STATIC)
+    assert abs(Jb[0] - Jd) <= 1e-12 * abs(Jd)
+    assert rel_inf(sb[0], sd) < 1e-12

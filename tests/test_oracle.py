@@ -62,6 +62,23 @@ def test_wang_schedule_of_the_library_host_code(lib):
         assert G.wang_recompute_count(int(N), int(K)) == rec, (N, K)
 
 
+def test_static_schedule_known_answers(orc, lib):
+    """StaticCheckpointing(K, N + 1): the oracle's restatement and the library's
+    host schedule against the table made by the reference's own
+    staticCheckpointing.cc (recomputed steps, exact reversal, states kept)."""
+    table = np.loadtxt(os.path.join(GOLD, "static_schedule.txt"), dtype=np.int64)
+    assert len(table) >= 70
+    for N, K, rec, ok, saved in table:
+        assert ok == 1
+        assert orc.static_count(int(N), int(K)) == (rec, True, saved), (N, K)
+        assert G.schedule_count(int(N), int(K), G.SCHEDULE_STATIC) == (rec, saved), (N, K)
+    ref = reference()
+    if ref is not None:   # where the reference tree exists: a wider sweep
+        for N in (5, 33, 257, 3000):
+            for K in (2, 5, 9, 40):
+                assert orc.static_count(N, K) == ref.static_count(N, K), (N, K)
+
+
 def test_oracle_matches_reference_build_on_fresh_inputs(orc):
     ref = reference()
     if ref is None:

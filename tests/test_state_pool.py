@@ -31,11 +31,14 @@ CASES = [(1, 2), (2, 2), (7, 2), (10, 3), (25, 4), (60, 7), (100, 5), (257, 16),
          (400, 64), (1000, 8), (2000, 64), (5000, 64)]
 
 
+@pytest.mark.parametrize("planned", [False, True], ids=["dynamic", "static"])
 @pytest.mark.parametrize("nsteps,nsnap", CASES)
-def test_zero_copy_schedule(sim, orc, nsteps, nsnap):
-    out = subprocess.run([sim, str(nsteps), str(nsnap)], capture_output=True, text=True)
+def test_zero_copy_schedule(sim, orc, nsteps, nsnap, planned):
+    out = subprocess.run([sim, str(nsteps), str(nsnap)] + (["static"] if planned else []),
+                         capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     tag, copies, recomputed = out.stdout.split()
     assert tag == "ok"
     assert int(copies) == 0
-    assert int(recomputed) == orc.wang_count(nsteps, nsnap)[0]
+    expect = orc.static_count(nsteps, nsnap)[0] if planned else orc.wang_count(nsteps, nsnap)[0]
+    assert int(recomputed) == expect
