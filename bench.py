@@ -204,6 +204,29 @@ def host_threads():
     return int(o.lib.orc_max_threads())
 
 
+def cpu_model():
+    """The host CPU as /proc/cpuinfo or lscpu names it (x86 'model name', Arm
+    'CPU part' / lscpu 'Model name'), with the online core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Vendor ID") and ":" in ln:
+                v = ln.split(":", 1)[1].strip()
+                name = v if name is None else name + " " + v
+    except Exception:
+        pass
+    if not name:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith(("model name", "cpu part")):
+                    name = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            name = "unknown"
+    return "%s, %d online cores" % (name, os.cpu_count() or 0)
+
+
 def slab_case(nz_slab):
     import workloads as W
     cfg, g, _ = W.workload_config3(W.STORE_FP64, nx=NX, ny=NY, nz=nz_slab, nsteps=NSTEPS_GRAD)
@@ -220,6 +243,7 @@ def cpu_baseline_leg():
     tf, ta = cpu_time(cfg, g, n, 1)
     mlups = cfg.ncells * n / (tf + ta) / 1e6
     return {"value": round(mlups, 4), "unit": "MLUPS", "cores": 1, "kind": "port",
+            "cpu": cpu_model(),
             "sample": "oracle (C restatement of the reference operators, FP64, 1 thread) on a "
                       "256x128x16 slab of the duct, %d forward + %d adjoint steps (%.1f s); "
                       "fwd %.3f / adj %.3f MLUPS" % (n, n, tf + ta, cfg.ncells * n / tf / 1e6,
@@ -247,6 +271,7 @@ def reference_arm(args, world, rank):
                                                        "FP64 (reference CPU path)"),
                        "sample": "256x128x16 slab per step"},
             "cpu_baseline": {"value": round(v, 4), "unit": "MLUPS", "cores": nthr, "kind": "port",
+                             "cpu": cpu_model(),
                              "sample": "oracle (C restatement of the reference operators, FP64, "
                                        "OpenMP %d threads): 1 forward + 1 adjoint step of a "
                                        "256x128x16 slab of the duct per bench step" % nthr},
