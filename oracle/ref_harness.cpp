@@ -35,6 +35,7 @@
 #include "adjointDynamics/reverseMRT3d.hh"
 #include "topOpt/dynamicCheckpointing.hh"
 #include "topOpt/staticCheckpointing.hh"
+#include "topOpt/MMA.hh"
 
 #include "../include/lbmgpu.h"
 
@@ -669,6 +670,57 @@ int ref_static_count(int nsteps, int nsnap, long long* recomputed, int* ok, int*
   *recomputed = ck.recomputed;
   if (ok) *ok = good;
   return 0;
+}
+
+/* The reference's MMA (topOpt/MMA.hh:111-229) on plain arrays: one object
+ * kept across updates so the asymptotes adapt as in an optimisation loop. */
+struct ref_mma {
+  MMA* mma = nullptr;
+  int n = 0, m = 0;
+  _p_Vec x, df0;
+  std::vector<_p_Vec> dg;
+};
+
+void* ref_mma_create(int n, int m, const double* x0, const double* robust_a) {
+  ref_mma* r = new ref_mma;
+  r->n = n;
+  r->m = m;
+  r->x.v.assign(x0, x0 + n);
+  r->df0.v.assign(n, 0.);
+  r->dg.resize(m);
+  for (auto& v : r->dg) v.v.assign(n, 0.);
+  r->mma = new MMA(n, m, &r->x);
+  if (robust_a) {
+    std::vector<double> a(robust_a, robust_a + m);
+    r->mma->SetRobustConstants(a.data());
+  }
+  return r;
+}
+
+/* x <- MMA update (Update with the outer move limit on [0,1]); *change = max |x_new - x_old| */
+int ref_mma_update(void* h, double* x, const double* df0dx, const double* g, const double* dgdx,
+                   double movlim, double* change) {
+  ref_mma* r = (ref_mma*)h;
+  std::memcpy(r->x.v.data(), x, sizeof(double) * r->n);
+  std::memcpy(r->df0.v.data(), df0dx, sizeof(double) * r->n);
+  std::vector<Vec> dgv(r->m);
+  for (int j = 0; j < r->m; ++j) {
+    std::memcpy(r->dg[j].v.data(), dgdx + (size_t)j * r->n, sizeof(double) * r->n);
+    dgv[j] = &r->dg[j];
+  }
+  std::vector<double> gv(g, g + r->m);
+  int rc = r->mma->Update(&r->x, &r->df0, gv.data(), dgv.data(), movlim);
+  double ch = 0.;
+  r->mma->DesignChange(&r->x, ch);
+  if (change) *change = ch;
+  std::memcpy(x, r->x.v.data(), sizeof(double) * r->n);
+  return rc;
+}
+
+void ref_mma_destroy(void* h) {
+  ref_mma* r = (ref_mma*)h;
+  delete r->mma;
+  delete r;
 }
 
 }  // extern "C"

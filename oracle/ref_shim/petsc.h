@@ -96,4 +96,73 @@ inline PetscErrorCode VecDestroyVecs(PetscInt n, Vec** vs) {
   return 0;
 }
 
+/* One-rank vector algebra used by the reference's MMA (topOpt/MMA.cc). */
+#define MPIU_SCALAR 0
+#define MPI_SUM 1
+#define MPI_MAX 2
+inline int MPI_Allreduce(const void* in, void* out, int n, int, int, MPI_Comm) {
+  if (in != out) std::memmove(out, in, sizeof(PetscScalar) * (size_t)n);
+  return 0;
+}
+#define PetscAbsReal(x) std::fabs(x)
+inline PetscErrorCode PetscPrintf(MPI_Comm, const char*, ...) { return 0; }
+inline PetscErrorCode PetscErrorPrintf(const char*, ...) { return 0; }
+inline PetscErrorCode VecDuplicate(Vec a, Vec* out) {
+  *out = new _p_Vec;
+  (*out)->v.assign(a->v.size(), 0.);
+  return 0;
+}
+inline PetscErrorCode VecDestroy(Vec* a) {
+  delete *a;
+  *a = nullptr;
+  return 0;
+}
+inline PetscErrorCode VecGetLocalSize(Vec a, PetscInt* n) {
+  *n = (PetscInt)a->v.size();
+  return 0;
+}
+inline PetscErrorCode VecGetSize(Vec a, PetscInt* n) { return VecGetLocalSize(a, n); }
+inline PetscErrorCode VecGetArray(Vec a, PetscScalar** p) {
+  *p = a->v.data();
+  return 0;
+}
+inline PetscErrorCode VecRestoreArray(Vec, PetscScalar** p) {
+  *p = nullptr;
+  return 0;
+}
+inline PetscErrorCode VecGetArrayRead(Vec a, const PetscScalar** p) {
+  *p = a->v.data();
+  return 0;
+}
+inline PetscErrorCode VecRestoreArrayRead(Vec, const PetscScalar** p) {
+  *p = nullptr;
+  return 0;
+}
+inline PetscErrorCode VecGetArrays(const Vec* a, PetscInt n, PetscScalar*** p) {
+  *p = new PetscScalar*[n > 0 ? n : 1];
+  for (PetscInt i = 0; i < n; ++i) (*p)[i] = a[i]->v.data();
+  return 0;
+}
+inline PetscErrorCode VecRestoreArrays(const Vec*, PetscInt, PetscScalar*** p) {
+  delete[] * p;
+  *p = nullptr;
+  return 0;
+}
+inline PetscErrorCode VecSet(Vec a, PetscScalar v) {
+  for (auto& x : a->v) x = v;
+  return 0;
+}
+/* y = alpha x + y */
+inline PetscErrorCode VecAXPY(Vec y, PetscScalar alpha, Vec x) {
+  for (size_t i = 0; i < y->v.size(); ++i) y->v[i] = alpha * x->v[i] + y->v[i];
+  return 0;
+}
+/* z = alpha x + beta y + gamma z */
+inline PetscErrorCode VecAXPBYPCZ(Vec z, PetscScalar alpha, PetscScalar beta, PetscScalar gamma,
+                                  Vec x, Vec y) {
+  for (size_t i = 0; i < z->v.size(); ++i)
+    z->v[i] = alpha * x->v[i] + beta * y->v[i] + gamma * z->v[i];
+  return 0;
+}
+
 #endif

@@ -80,6 +80,12 @@ def main():
                header="nsteps nsnapshots recomputed_steps reversal_exact saved_states "
                       "(reference StaticCheckpointing(K, nsteps + 1) + WangCheckpointing)")
     print("static table", len(table))
+    # the reference's MMA (topOpt/MMA.cc) on the seeded problems of design_lib
+    import design_lib as D
+    for kind in ("plain", "minmax"):
+        xs, chs = D.mma_trajectory(D.ReferenceMMA, kind)
+        np.savez_compressed(os.path.join(HERE, "mma_%s.npz" % kind), x=xs, change=chs)
+        print("mma", kind, "final change", chs[-1])
 
 
 if __name__ == "__main__":
