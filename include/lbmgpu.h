@@ -156,6 +156,17 @@ int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop);
  * LBSolver::setFieldFromDesignVec (latticeBoltzmann/LBSolver.cc:333-348). */
 int lbm_set_design(lbm_handle* h, const double* gamma);
 
+/* lbm_set_design from device memory (ncells FP64 values on the current
+ * device, e.g. the output of lbm_topopt_apply's filter chain); waits for the
+ * device to finish the caller's work first.  The values are not checked for
+ * range.  No reference counterpart (the reference's design vectors are host
+ * PETSc Vecs). */
+int lbm_set_design_device(lbm_handle* h, const double* gamma_dev);
+
+/* Device address of the handle's FP64 dJ/dgamma (ncells values, valid until
+ * the handle is destroyed; its contents change with the next reverse step). */
+int lbm_get_sensitivity_device(const lbm_handle* h, const double** sens_dev);
+
 /* f_0 = feq(macros) and t = 0.  macros: NULL for rho=1, u=0 (T=0), else
  * per cell {rho,ux,uy} (D2Q9), {rho,ux,uy,uz} (D3Q19) or {rho,ux,uy,T}.
  * Replaces LBSolver::initializeAtEquilibrium (LBSolver.cc:234-249). */
@@ -304,6 +315,79 @@ int lbm_batch_gradient_schedule(lbm_batch* b, int nsteps, int nsnapshots, int sc
 /* As lbm_time_steps, for the batched kernels. */
 int lbm_batch_time_steps(lbm_batch* b, int which, int nsteps, float* ms);
 int lbm_batch_get_launch_count(const lbm_batch* b, int64_t* launches);
+
+/* ------------------------------------------------------------------------
+ * Design update on the device: the reference's optimisation loop around the
+ * solver (applications/RobustPump2d/robustPump2d.cc:215-315) without host
+ * round trips.  Design variables x live on the cells of a design box
+ * (FullToDesignMapping2d, topOpt/fullToDesignMapping2d.cc); the full field
+ * (a fixed background outside the box) passes up to two density-filter +
+ * tanh-projection stages (DensityFilter2d/3d, ProjectionFilter2d,
+ * DoubleProjectionFilter2d) to the physical gamma; sensitivities go back
+ * through the transposed chain; a volume constraint (VolumeConstraint,
+ * functionals/volumeConstraint.cc) and MMA (Svanberg 1987, with the
+ * subproblem of topOpt/MMA.cc) update x.  Several realisations (robust
+ * design: the last projection's eta per realisation) give the min-max form
+ * of robustPump2d.cc:166-190 (constraints J_r + magic - z <= 0).  FP64
+ * throughout.
+ * ------------------------------------------------------------------------ */
+#define LBM_VOLUME_NONE 0
+#define LBM_VOLUME_FLUID 1    /* ConstrainFluid:    mean(gamma) - V <= 0 */
+#define LBM_VOLUME_MATERIAL 2 /* ConstrainMaterial: (1 - V) - mean(gamma) <= 0 */
+#define LBM_MAX_STAGES 2
+#define LBM_MAX_REALISATIONS 8
+
+typedef struct lbm_topopt_config {
+  int nx, ny, nz;             /* the lattice (nz = 1 in 2D) */
+  int design_box[6];          /* x0,x1,y0,y1,z0,z1 (inclusive): one design variable per cell */
+  int nstages;                /* 0, 1 or 2 filter stages */
+  int radius[LBM_MAX_STAGES]; /* cone filter radius of each stage (cells) */
+  int filter_box[6];          /* rows the filters act on (the reference passes the design box) */
+  int project[LBM_MAX_STAGES];/* 1: tanh projection after the stage's filter */
+  double beta[LBM_MAX_STAGES], eta[LBM_MAX_STAGES];
+  int nreal;                  /* realisations: 1 = minimise J; > 1 = minimise max_r J_r */
+  double real_eta[LBM_MAX_REALISATIONS]; /* eta of the last projection per realisation (nreal > 1) */
+  int volume_type;            /* LBM_VOLUME_* */
+  double volume;              /* V */
+  int volume_real;            /* realisation whose physical field the volume is measured on */
+  double move_limit;          /* MMA outer move limit (MMA::Update's movlim) */
+  double magic;               /* added to every J_r in the min-max form (robustPump2d.cc:182) */
+} lbm_topopt_config;
+
+typedef struct lbm_topopt lbm_topopt;
+
+/* Defaults: one stage of radius 2 with projection beta 1, eta 0.5;
+ * ConstrainFluid at 0.5; move limit 0.1; magic 5; nreal 1. */
+void lbm_topopt_config_default(lbm_topopt_config* c);
+/* background: full-grid gamma outside the design box (NULL = 1, fluid);
+ * x0: initial design variables (NULL = 0.5). */
+int lbm_topopt_create(const lbm_topopt_config* c, const double* background, const double* x0,
+                      lbm_topopt** out);
+int lbm_topopt_destroy(lbm_topopt* t);
+const char* lbm_topopt_last_error(const lbm_topopt* t);
+int lbm_topopt_num_variables(const lbm_topopt* t, int64_t* n);
+int lbm_topopt_set_variables(lbm_topopt* t, const double* x);
+int lbm_topopt_get_variables(const lbm_topopt* t, double* x);
+/* ProjectionFilter2d::setBeta / increaseBeta (projectionFilter2d.hh:16-18) */
+int lbm_topopt_set_beta(lbm_topopt* t, int stage, double beta);
+/* Physical field of realisation r (host copy, nx*ny*nz values). */
+int lbm_topopt_physical(lbm_topopt* t, int r, double* gamma);
+/* Physical field of realisation r into a handle's design, on the device
+ * (filterDesign + setFieldFromDesignVec). */
+int lbm_topopt_apply(lbm_topopt* t, int r, lbm_handle* h);
+/* Objective J_r and the handle's dJ/dgamma (after lbm_gradient) for
+ * realisation r: the chain rule through the filters and the box
+ * (filterSensitivities + mapFullToDesign), on the device. */
+int lbm_topopt_set_sensitivity(lbm_topopt* t, int r, lbm_handle* h, double J);
+/* The same from a host dJ/dgamma (nx*ny*nz values). */
+int lbm_topopt_set_sensitivity_host(lbm_topopt* t, int r, const double* dJdgamma, double J);
+/* dJ_r/dx (host copy, one value per design variable). */
+int lbm_topopt_get_design_sensitivity(const lbm_topopt* t, int r, double* dJdx);
+/* Volume constraint and one MMA step (MMA::Update + DesignChange): x is
+ * replaced; *change = max |x_new - x_old|; constraints (may be NULL) gets the
+ * constraint values handed to MMA (nreal == 1: the volume; else J_r + magic
+ * for every r, then the volume). */
+int lbm_topopt_update(lbm_topopt* t, double* change, double* constraints);
 
 /* Objective weight*F(f_t) of a state that lives in the caller's own device
  * memory, computed without allocating any device memory.  For callers that

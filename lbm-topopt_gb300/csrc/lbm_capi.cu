@@ -629,6 +629,26 @@ int lbm_set_design(lbm_handle* h, const double* gamma) {
   return LBM_OK;
 }
 
+int lbm_set_design_device(lbm_handle* h, const double* gamma_dev) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (!gamma_dev) return fail(h, LBM_ERR_ARG, "null design pointer");
+  // the caller's producing work must be complete before this stream reads it
+  CUDA_OR_FAIL(h, cudaDeviceSynchronize());
+  KParams p = base_params(h, 0);
+  int rc = launch(h, K_GAMMA, p, const_cast<double*>(gamma_dev));
+  if (rc) return rc;
+  rc = sync(h);
+  if (rc) return rc;
+  h->have_design = true;
+  return LBM_OK;
+}
+
+int lbm_get_sensitivity_device(const lbm_handle* h, const double** sens_dev) {
+  if (!h || !sens_dev) return fail(nullptr, LBM_ERR_ARG, "null argument");
+  *sens_dev = h->sens;
+  return LBM_OK;
+}
+
 int lbm_init_equilibrium(lbm_handle* h, const double* macros) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
   if (macros) {

@@ -209,6 +209,22 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_autotune": (C.c_int, [H, C.c_int]),
         "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
+        "lbm_set_design_device": (C.c_int, [H, C.c_void_p]),
+        "lbm_get_sensitivity_device": (C.c_int, [H, C.POINTER(C.c_void_p)]),
+        "lbm_topopt_config_default": (None, [C.c_void_p]),
+        "lbm_topopt_create": (C.c_int, [C.c_void_p, dp, dp, C.POINTER(C.c_void_p)]),
+        "lbm_topopt_destroy": (C.c_int, [C.c_void_p]),
+        "lbm_topopt_last_error": (C.c_char_p, [C.c_void_p]),
+        "lbm_topopt_num_variables": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+        "lbm_topopt_set_variables": (C.c_int, [C.c_void_p, dp]),
+        "lbm_topopt_get_variables": (C.c_int, [C.c_void_p, dp]),
+        "lbm_topopt_set_beta": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+        "lbm_topopt_physical": (C.c_int, [C.c_void_p, C.c_int, dp]),
+        "lbm_topopt_apply": (C.c_int, [C.c_void_p, C.c_int, H]),
+        "lbm_topopt_set_sensitivity": (C.c_int, [C.c_void_p, C.c_int, H, C.c_double]),
+        "lbm_topopt_set_sensitivity_host": (C.c_int, [C.c_void_p, C.c_int, dp, C.c_double]),
+        "lbm_topopt_get_design_sensitivity": (C.c_int, [C.c_void_p, C.c_int, dp]),
+        "lbm_topopt_update": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), dp]),
         "lbm_wang_recompute_count": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64)]),
         "lbm_schedule_count": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64)]),
@@ -473,6 +489,124 @@ class Batch:
 
 
 # -- reference-style facades -----------------------------------------------------
+
+# -- design update on the device --------------------------------------------------
+
+VOLUME_NONE, VOLUME_FLUID, VOLUME_MATERIAL = 0, 1, 2
+MAX_STAGES, MAX_REALISATIONS = 2, 8
+
+
+class CTopOptConfig(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("design_box", C.c_int * 6), ("nstages", C.c_int),
+                ("radius", C.c_int * MAX_STAGES), ("filter_box", C.c_int * 6),
+                ("project", C.c_int * MAX_STAGES), ("beta", C.c_double * MAX_STAGES),
+                ("eta", C.c_double * MAX_STAGES), ("nreal", C.c_int),
+                ("real_eta", C.c_double * MAX_REALISATIONS), ("volume_type", C.c_int),
+                ("volume", C.c_double), ("volume_real", C.c_int), ("move_limit", C.c_double),
+                ("magic", C.c_double)]
+
+
+class TopOpt:
+    """The design update of the optimisation loop on the device (lbm_topopt_*):
+    design variables on a box, up to two density-filter + tanh-projection
+    stages to the physical gamma, their transposes, a volume constraint and
+    MMA.  stages: list of (radius, project, beta, eta)."""
+
+    def __init__(self, nx, ny, nz, design_box, stages=((2, True, 1.0, 0.5),), filter_box=None,
+                 nreal=1, real_eta=None, volume_type=VOLUME_FLUID, volume=0.5, volume_real=0,
+                 move_limit=0.1, magic=5.0, background=None, x0=None):
+        self.lib = load_library()
+        lib = self.lib
+        c = CTopOptConfig()
+        lib.lbm_topopt_config_default(C.byref(c))
+        c.nx, c.ny, c.nz = int(nx), int(ny), int(nz)
+        c.design_box[:] = [int(v) for v in design_box]
+        c.filter_box[:] = [int(v) for v in (filter_box if filter_box is not None else design_box)]
+        c.nstages = len(stages)
+        for k, (r, proj, beta, eta) in enumerate(stages):
+            c.radius[k], c.project[k], c.beta[k], c.eta[k] = int(r), int(bool(proj)), beta, eta
+        c.nreal = int(nreal)
+        for r, e in enumerate(real_eta or []):
+            c.real_eta[r] = e
+        c.volume_type, c.volume, c.volume_real = int(volume_type), float(volume), int(volume_real)
+        c.move_limit, c.magic = float(move_limit), float(magic)
+        self.cfg = c
+        self.ncells = int(nx) * int(ny) * int(nz)
+        self.t = C.c_void_p()
+        bg = None if background is None else np.ascontiguousarray(background, dtype=np.float64)
+        xx = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+        rc = lib.lbm_topopt_create(C.byref(c), _ptr(bg), _ptr(xx), C.byref(self.t))
+        if rc:
+            raise LBMError(rc, lib.lbm_last_error(None).decode())
+        n = C.c_int64()
+        self._check(lib.lbm_topopt_num_variables(self.t, C.byref(n)))
+        self.n = n.value
+        self.nreal = int(nreal)
+
+    def _check(self, rc):
+        if rc:
+            raise LBMError(rc, self.lib.lbm_topopt_last_error(self.t).decode())
+
+    def close(self):
+        if self.t:
+            self.lib.lbm_topopt_destroy(self.t)
+            self.t = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_variables(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        assert x.size == self.n
+        self._check(self.lib.lbm_topopt_set_variables(self.t, _ptr(x)))
+
+    def variables(self):
+        x = np.empty(self.n)
+        self._check(self.lib.lbm_topopt_get_variables(self.t, _ptr(x)))
+        return x
+
+    def set_beta(self, stage, beta):
+        self._check(self.lib.lbm_topopt_set_beta(self.t, int(stage), float(beta)))
+
+    def physical(self, r=0):
+        g = np.empty(self.ncells)
+        self._check(self.lib.lbm_topopt_physical(self.t, int(r), _ptr(g)))
+        return g
+
+    def apply(self, r, handle):
+        self._check(self.lib.lbm_topopt_apply(self.t, int(r), handle.h))
+
+    def set_sensitivity(self, r, handle, J):
+        self._check(self.lib.lbm_topopt_set_sensitivity(self.t, int(r), handle.h, float(J)))
+
+    def set_sensitivity_host(self, r, dJdgamma, J):
+        s = np.ascontiguousarray(dJdgamma, dtype=np.float64)
+        assert s.size == self.ncells
+        self._check(self.lib.lbm_topopt_set_sensitivity_host(self.t, int(r), _ptr(s), float(J)))
+
+    def design_sensitivity(self, r=0):
+        d = np.empty(self.n)
+        self._check(self.lib.lbm_topopt_get_design_sensitivity(self.t, int(r), _ptr(d)))
+        return d
+
+    def update(self):
+        """One volume-constraint + MMA step; returns (change, constraint values)."""
+        ch = C.c_double()
+        g = np.zeros(MAX_REALISATIONS + 1)
+        self._check(self.lib.lbm_topopt_update(self.t, C.byref(ch), _ptr(g)))
+        m = (self.nreal if self.nreal > 1 else 0) + (1 if self.cfg.volume_type else 0)
+        return ch.value, g[:m].copy()
+
 
 class IsothermalLBSolver:
     """Mirror of IsothermalLBSolver2d/3d (latticeBoltzmann/isothermalLBSolver2d.hh:20-110)."""
