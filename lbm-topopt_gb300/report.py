@@ -17,6 +17,9 @@
 5  8 D2Q9 lattices (3 projected designs of 1024x512 + 5 uneven ones), 4000
    steps: batched gradient (one launch per step, CUDA graph) against the same
    lattices one at a time.
+6  robust design iteration on the device: 3 realisations of the 1024x512
+   channel, double projection filter, batched gradient, chain rule and one
+   min-max MMA step, with the CPU oracle's filter and MMA beside it.
 """
 import argparse
 import json
@@ -191,12 +194,88 @@ def config5(quick):
             "max_J_rel_diff_batched_vs_single": float(max(abs(a - b) / abs(b) for a, b in zip(J, Js)))}
 
 
+def config6(quick):
+    """Robust design iteration at the batch scale: three realisations (the
+    second projection's eta 0.3 / 0.5 / 0.7) of the 1024x512 channel, the
+    double projection filter of RobustPump2d (radii 8 and 4), one batched
+    FP32 gradient, the chain rule of each realisation and one min-max MMA step
+    with a fluid-volume constraint, all on the device; the CPU oracle's filter
+    chain and MMA on the same inputs for comparison."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import design_lib as D
+    n = 400 if quick else 4000
+    nx, ny = 1024, 512
+    cfg = W.channel_2d(nx, ny, storage=G.STORE_FP32, nsteps=n)
+    box = (32, nx - 33, 1, ny - 2, 0, 0)
+    stages = [(8, True, 2.0, 0.5), (4, True, 1.0, 0.5)]
+    etas = [0.3, 0.5, 0.7]
+    mask = np.zeros((ny, nx), bool)
+    mask[box[2]:box[3] + 1, box[0]:box[1] + 1] = True
+    x0 = W.design_2d(nx, ny, W.SEED_BASE + 6).reshape(ny, nx)[mask]
+    x0 = np.clip(x0, 0.0, 1.0)
+    out = {"config": 6, "workload": "robust design iteration: 3 realisations of a 1024x512 D2Q9 "
+                                    "channel, double projection (R 8 + 4), FP32 gradient of %d "
+                                    "steps, min-max MMA with a fluid-volume constraint" % n,
+           "design_variables": int(mask.sum())}
+    with G.TopOpt(nx, ny, 1, box, stages, nreal=3, real_eta=etas, volume_type=G.VOLUME_FLUID,
+                  volume=0.8, move_limit=0.1, x0=x0) as t, G.Batch([cfg] * 3) as b:
+        times = {}
+
+        def iteration(record):
+            t0 = time.perf_counter()
+            for r in range(3):
+                t.apply(r, b[r])
+            t1 = time.perf_counter()
+            J, _, _ = b.gradient(n, 64, use_graph=True)
+            t2 = time.perf_counter()
+            for r in range(3):
+                t.set_sensitivity(r, b[r], J[r])
+            t3 = time.perf_counter()
+            sens = [t.design_sensitivity(r) for r in range(3)]
+            xb = t.variables()
+            t4 = time.perf_counter()
+            ch, cons = t.update()
+            t5 = time.perf_counter()
+            if record:
+                times.update(apply_s=t1 - t0, gradient_s=t2 - t1, chain_rule_s=t3 - t2,
+                             mma_update_s=t5 - t4, iteration_s=(t3 - t0) + (t5 - t4))
+            return J, sens, xb, cons, ch
+
+        J, sens, xb, cons, ch = iteration(False)          # graph capture on the first pass
+        xa = t.variables()
+        # the same first update on the CPU oracle
+        a_const = np.array([1., 1., 1., 0.])
+        # realisation 0's chain (the volume is measured on it): last eta = etas[0]
+        st0 = [(r_, box, p_, b_, e_) for r_, p_, b_, e_ in stages]
+        st0[-1] = st0[-1][:4] + (etas[0],)
+        ch_o = D.make_chain(nx, ny, 1, st0)
+        tc0 = time.perf_counter()
+        xfull = np.ones(nx * ny)
+        xfull[mask.reshape(-1)] = xb
+        D.filter_forward(ch_o, xfull)
+        tc1 = time.perf_counter()
+        dvol = np.full(nx * ny, 1.0 / mask.sum())
+        dvol_x = D.filter_transpose(ch_o, xfull, dvol)[mask.reshape(-1)]
+        tc2 = time.perf_counter()
+        orc = D.OracleMMA(len(xb), 4, xb, a_const)
+        dg = np.vstack(sens + [dvol_x])
+        x_o, _, _ = orc.update(xb, np.zeros(len(xb)), cons, dg, 0.1)
+        tc3 = time.perf_counter()
+        out.update(J=[float(v) for v in J], constraints=[float(v) for v in cons],
+                   first_change=ch, mma_gpu_vs_oracle_max_abs=float(np.abs(xa - x_o).max()),
+                   cpu_filter_forward_s=tc1 - tc0, cpu_filter_transpose_s=tc2 - tc1,
+                   cpu_mma_update_s=tc3 - tc2)
+        iteration(True)
+        out.update(times)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--configs", type=int, nargs="*", default=[1, 2, 3, 4, 5])
+    ap.add_argument("--configs", type=int, nargs="*", default=[1, 2, 3, 4, 5, 6])
     ap.add_argument("--quick", action="store_true", help="shorter horizons")
     a = ap.parse_args()
-    fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5}
+    fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5, 6: config6}
     for c in a.configs:
         t0 = time.perf_counter()
         r = fns[c](a.quick)
