@@ -179,6 +179,17 @@ int lbm_init_equilibrium(lbm_handle* h, const double* macros);
  * LBSolver::computeMacroFunctional (LBSolver.cc:74-91). */
 int lbm_forward(lbm_handle* h, int nsteps, double* J_steps, double* J_sum);
 
+/* Advance until the state is steady: every check_every steps the largest
+ * change of any population over the last step, max |f_t - f_{t-1}|, is
+ * measured on the device; stop when it is below tol, or after max_steps
+ * steps (then the change of the last step is measured as well).  No
+ * objective is evaluated.  *steps (may be NULL) = steps taken, *change (may
+ * be NULL) = the last change measured.  Replaces the steady-state loop of
+ * applications/Regenerator2d/regenerator2d.cc:255-272 (chkFreq, tol,
+ * maxSteps); the unsteady part that follows there is lbm_forward. */
+int lbm_forward_steady(lbm_handle* h, int max_steps, int check_every, double tol, int* steps,
+                       double* change);
+
 /* Current time step t of the state. */
 int lbm_get_time(const lbm_handle* h, int* t);
 

@@ -4,6 +4,7 @@
 // is no host fallback.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -121,6 +122,38 @@ __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict_
     for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) tot += sh[w];
     *out = tot;
   }
+}
+
+// *bits = bit pattern of max |a - b| over the Q planes of ncell valid cells
+// (the padding at the end of each plane is skipped).  Non-negative doubles
+// order like their bit patterns, so an integer atomicMax finds the maximum in
+// any order; a NaN (positive pattern above every number) wins and is reported.
+template <class S>
+__global__ void k_max_change(const S* __restrict__ a, const S* __restrict__ b, int Q, long long P,
+                             long long ncell, unsigned long long* bits) {
+  double m = 0.;
+  const long long total = (long long)Q * ncell;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long q = i / ncell, c = i - q * ncell;
+    const double d = fabs((double)a[q * P + c] - (double)b[q * P + c]);
+    m = (d > m || d != d) ? d : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_down_sync(0xffffffffu, m, o);
+    m = (v > m || v != v) ? v : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(bits, (unsigned long long)__double_as_longlong(m));
+}
+
+void launch_max_change(size_t pop_bytes, const void* a, const void* b, int Q, long long P,
+                       long long ncell, unsigned long long* bits, unsigned blocks, cudaStream_t st) {
+  if (pop_bytes == 8)
+    k_max_change<double><<<blocks, 256, 0, st>>>((const double*)a, (const double*)b, Q, P, ncell, bits);
+  else if (pop_bytes == 4)
+    k_max_change<float><<<blocks, 256, 0, st>>>((const float*)a, (const float*)b, Q, P, ncell, bits);
+  else
+    k_max_change<__half><<<blocks, 256, 0, st>>>((const __half*)a, (const __half*)b, Q, P, ncell, bits);
 }
 
 size_t state_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->pop_bytes; }
@@ -665,6 +698,43 @@ int lbm_init_equilibrium(lbm_handle* h, const double* macros) {
   int rc = init_state(h);
   if (rc) return rc;
   return sync(h);
+}
+
+int lbm_forward_steady(lbm_handle* h, int max_steps, int check_every, double tol, int* steps,
+                       double* change) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (max_steps < 1 || check_every < 1) return fail(h, LBM_ERR_ARG, "need max_steps >= 1 and check_every >= 1");
+  if (!(tol >= 0.)) return fail(h, LBM_ERR_ARG, "tol must be >= 0");
+  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+  if (!h->have_state) return fail(h, LBM_ERR_STATE, "no state (lbm_init_equilibrium)");
+  int rc = ensure_jcap(h, 1);
+  if (rc) return rc;
+  unsigned long long* bits = (unsigned long long*)h->jdev;
+  double last = -1.;
+  int k = 0;
+  while (k < max_steps) {
+    if ((rc = forward_step(h, nullptr))) return rc;
+    ++k;
+    if (k % check_every == 0 || k == max_steps) {
+      // the step's input is intact in the other state buffer
+      CUDA_OR_FAIL(h, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), h->stream));
+      const long long total = (long long)h->Q * h->ncell;
+      const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 4096);
+      launch_max_change(h->pop_bytes, h->f[h->cur], h->f[1 - h->cur], h->Q, h->P, h->ncell, bits,
+                        blocks, h->stream);
+      CUDA_OR_FAIL(h, cudaGetLastError());
+      unsigned long long hb = 0;
+      CUDA_OR_FAIL(h, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
+      CUDA_OR_FAIL(h, cudaStreamSynchronize(h->stream));
+      memcpy(&last, &hb, sizeof(last));
+      if (!std::isfinite(last)) return fail(h, LBM_ERR_NONFINITE, "state is not finite at step %d", h->t);
+      if (last < tol) break;
+    }
+  }
+  if ((rc = sync(h))) return rc;
+  if (steps) *steps = k;
+  if (change) *change = last;
+  return LBM_OK;
 }
 
 int lbm_forward(lbm_handle* h, int nsteps, double* J_steps, double* J_sum) {

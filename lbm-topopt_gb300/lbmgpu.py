@@ -209,6 +209,8 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_autotune": (C.c_int, [H, C.c_int]),
         "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
+        "lbm_forward_steady": (C.c_int, [H, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_double)]),
         "lbm_set_design_device": (C.c_int, [H, C.c_void_p]),
         "lbm_get_sensitivity_device": (C.c_int, [H, C.POINTER(C.c_void_p)]),
         "lbm_topopt_config_default": (None, [C.c_void_p]),
@@ -387,6 +389,14 @@ class Handle:
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_get_launch_shape(self.h, int(which), C.byref(bx), C.byref(by)))
         return bx.value, by.value
+
+    def forward_steady(self, max_steps: int, check_every: int = 100, tol: float = 1e-6):
+        """Advance until max |f_t - f_{t-1}| < tol (tested every check_every
+        steps) or max_steps; returns (steps taken, last change)."""
+        n, ch = C.c_int(), C.c_double()
+        self._check(self.lib.lbm_forward_steady(self.h, int(max_steps), int(check_every),
+                                                float(tol), C.byref(n), C.byref(ch)))
+        return n.value, ch.value
 
     def set_launch_shape(self, which: int, bx: int, by: int):
         self._check(self.lib.lbm_set_launch_shape(self.h, int(which), int(bx), int(by)))

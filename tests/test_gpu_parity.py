@@ -308,3 +308,28 @@ def test_static_schedule_gives_the_same_gradient(orc):
         Jb, sb, _ = b.gradient(n, k, use_graph=True, schedule=G.SCHEDULE_STATIC)
     assert abs(Jb[0] - Jd) <= 1e-12 * abs(Jd)
     assert rel_inf(sb[0], sd) < 1e-12
+
+
+@pytest.mark.parametrize("storage,tol", [(G.STORE_FP64, 1e-9), (G.STORE_FP32, 1e-6)])
+def test_forward_until_steady(orc, storage, tol):
+    """The steady-state run of the regenerator application: it stops at a
+    check step once max |f_t - f_{t-1}| < tol, and has then taken exactly that
+    many steps (the state equals the oracle's after the same number of steps);
+    max_steps bounds it."""
+    cfg = W.channel_2d(48, 20, nsteps=100).replace(storage=storage)
+    gamma = W.design_2d(48, 20, 33)
+    with G.Handle(cfg) as h:
+        h.set_design(gamma)
+        h.init_equilibrium()
+        n, ch = h.forward_steady(40000, 100, tol)
+        assert n < 40000 and n % 100 == 0 and 0 <= ch < tol
+        assert h.time() == n
+        f = h.populations()
+        h.init_equilibrium()
+        n2, ch2 = h.forward_steady(250, 100, 0.0)   # never below 0: runs to max_steps
+        assert n2 == 250 and ch2 > 0
+    fo, _, _ = orc.forward(cfg.replace(storage=G.STORE_FP64), gamma, n)
+    lim = 1e-12 if storage == G.STORE_FP64 else 1e-5
+    assert rel_inf(f, fo) < lim
+    fp, _, _ = orc.forward(cfg.replace(storage=G.STORE_FP64), gamma, n - 1)
+    assert np.abs(fo - fp).max() < 10 * tol
