@@ -152,6 +152,9 @@ const char* lbm_last_error(const lbm_handle* h);
 /* Cells (nx*ny*nz) and populations per cell (9, 19 or 9+5). */
 int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop);
 
+/* Lattice dimensions {nx, ny, nz} (nz = 1 in 2D). */
+int lbm_get_dims(const lbm_handle* h, int dims[3]);
+
 /* Design field gamma in [0,1], one double per cell.  Replaces
  * LBSolver::setFieldFromDesignVec (latticeBoltzmann/LBSolver.cc:333-348). */
 int lbm_set_design(lbm_handle* h, const double* gamma);
@@ -426,6 +429,27 @@ int lbm_topopt_update(lbm_topopt* t, double* change, double* constraints);
  * Errors are reported through lbm_last_error(NULL). */
 int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f_dev,
                           const void* gamma_dev, double* J_dev, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Files, on the host (errors through lbm_last_error(NULL)).
+ * ------------------------------------------------------------------------ */
+
+/* PETSc binary Vec file, as writeVectorToBinary / loadVectorFromBinary
+ * (core/binaryIO.cc:3-33) write and read design vectors: big-endian int32
+ * class id 1211214, int32 length, big-endian doubles. */
+int lbm_write_petsc_vec(const char* path, const double* v, int64_t n);
+/* v may be NULL to query the length only; fails if the file holds more than
+ * n_max values. */
+int lbm_read_petsc_vec(const char* path, double* v, int64_t n_max, int64_t* n);
+
+/* VTK XML StructuredGrid (.vts) of point fields on an nx*ny*nz lattice (x
+ * fastest): field k has ncomp[k] components per point. */
+int lbm_write_vts_fields(const char* path, int nx, int ny, int nz, int nfields,
+                         const char* const* names, const int* ncomp, const double* const* data);
+/* The handle's macros at its current state (rho, velocity, and T for the
+ * thermal lattice) and, if gamma is not NULL, the design field, as .vts:
+ * LBSolver::outputMacros / outputFields (latticeBoltzmann/LBSolver.cc:251-286). */
+int lbm_write_vts(lbm_handle* h, const char* path, const double* gamma);
 
 #ifdef __cplusplus
 }

@@ -634,6 +634,14 @@ int lbm_destroy(lbm_handle* h) {
   return LBM_OK;
 }
 
+int lbm_get_dims(const lbm_handle* h, int dims[3]) {
+  if (!h || !dims) return fail(nullptr, LBM_ERR_ARG, "null argument");
+  dims[0] = h->cfg.nx;
+  dims[1] = h->cfg.ny;
+  dims[2] = h->dim == 3 ? h->cfg.nz : 1;
+  return LBM_OK;
+}
+
 int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
   if (ncells) *ncells = h->ncell;

@@ -211,6 +211,13 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
         "lbm_forward_steady": (C.c_int, [H, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int),
                                          C.POINTER(C.c_double)]),
+        "lbm_get_dims": (C.c_int, [H, C.POINTER(C.c_int)]),
+        "lbm_write_petsc_vec": (C.c_int, [C.c_char_p, dp, C.c_int64]),
+        "lbm_read_petsc_vec": (C.c_int, [C.c_char_p, dp, C.c_int64, C.POINTER(C.c_int64)]),
+        "lbm_write_vts_fields": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(C.c_char_p), C.POINTER(C.c_int),
+                                           C.POINTER(dp)]),
+        "lbm_write_vts": (C.c_int, [H, C.c_char_p, dp]),
         "lbm_set_design_device": (C.c_int, [H, C.c_void_p]),
         "lbm_get_sensitivity_device": (C.c_int, [H, C.POINTER(C.c_void_p)]),
         "lbm_topopt_config_default": (None, [C.c_void_p]),
@@ -267,6 +274,41 @@ def schedule_count(nsteps: int, nsnapshots: int, schedule: int = SCHEDULE_DYNAMI
     if rc:
         raise LBMError(rc, lib.lbm_last_error(None).decode())
     return rec.value, saved.value
+
+
+def _io_check(lib, rc):
+    if rc:
+        raise LBMError(rc, lib.lbm_last_error(None).decode())
+
+
+def write_petsc_vec(path: str, v) -> None:
+    """PETSc binary Vec file (writeVectorToBinary)."""
+    lib = load_library()
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    _io_check(lib, lib.lbm_write_petsc_vec(path.encode(), _ptr(v), v.size))
+
+
+def read_petsc_vec(path: str) -> np.ndarray:
+    """PETSc binary Vec file (loadVectorFromBinary)."""
+    lib = load_library()
+    n = C.c_int64()
+    _io_check(lib, lib.lbm_read_petsc_vec(path.encode(), None, 0, C.byref(n)))
+    v = np.empty(n.value)
+    _io_check(lib, lib.lbm_read_petsc_vec(path.encode(), _ptr(v), v.size, C.byref(n)))
+    return v
+
+
+def write_vts(path: str, dims, fields) -> None:
+    """VTK XML StructuredGrid of point fields: fields = {name: array of
+    ncells * ncomp values} (ncomp inferred)."""
+    lib = load_library()
+    nx, ny, nz = (list(dims) + [1, 1])[:3]
+    ncell = nx * ny * nz
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in fields.values()]
+    names = (C.c_char_p * len(arrs))(*[k.encode() for k in fields])
+    comps = (C.c_int * len(arrs))(*[a.size // ncell for a in arrs])
+    ptrs = (C.POINTER(C.c_double) * len(arrs))(*[_ptr(a) for a in arrs])
+    _io_check(lib, lib.lbm_write_vts_fields(path.encode(), nx, ny, nz, len(arrs), names, comps, ptrs))
 
 
 def wang_recompute_count(nsteps: int, nsnapshots: int) -> int:
@@ -389,6 +431,16 @@ class Handle:
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_get_launch_shape(self.h, int(which), C.byref(bx), C.byref(by)))
         return bx.value, by.value
+
+    def dims(self):
+        d = (C.c_int * 3)()
+        self._check(self.lib.lbm_get_dims(self.h, d))
+        return tuple(d)
+
+    def write_vts(self, path: str, gamma=None):
+        """Macros of the current state (and gamma) as a .vts file."""
+        g = None if gamma is None else np.ascontiguousarray(gamma, dtype=np.float64)
+        self._check(self.lib.lbm_write_vts(self.h, path.encode(), _ptr(g)))
 
     def forward_steady(self, max_steps: int, check_every: int = 100, tol: float = 1e-6):
         """Advance until max |f_t - f_{t-1}| < tol (tested every check_every
