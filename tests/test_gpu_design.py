@@ -8,6 +8,8 @@
   dJ/dx against central differences on a channel, FP64;
 * a short optimisation loop lowers the objective and meets the volume
   constraint."""
+import os
+
 import numpy as np
 import pytest
 
@@ -142,3 +144,23 @@ def test_short_optimisation_lowers_the_pressure_drop():
         assert abs(vols[-1]) < 0.02
         x = t.variables()
         assert x.min() >= 0 and x.max() <= 1
+
+
+def test_robust_minmax_loop(tmp_path):
+    """The robust loop of optimize.py (3 realisations in one batch, double
+    projection, static checkpoints, min-max MMA): the worst case falls, the
+    realisations keep the order of their eta (a larger eta projects less
+    fluid, so a larger pressure drop), the volume constraint ends near
+    active, and the designs and fields are written."""
+    import optimize as O
+    x, hist = O.optimise(64, 32, 120, iters=15, robust=True, volume=0.6, nsnap=8,
+                         storage=G.STORE_FP64, out_dir=str(tmp_path), every=10, log=lambda s: None)
+    worst = [max(h["J"]) for h in hist]
+    assert worst[-1] < worst[0]
+    J = hist[-1]["J"]
+    assert J[0] <= J[1] <= J[2]
+    assert abs(hist[-1]["volume"]) < 0.05
+    files = sorted(os.listdir(tmp_path))
+    assert "design_iter_0.bin" in files and "fields_iter_0.vts" in files
+    v = G.read_petsc_vec(str(tmp_path / "design_iter_0.bin"))
+    assert v.size == x.size
