@@ -32,7 +32,10 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 NX, NY, NZ = 256, 128, 128
 NSTEPS_GRAD = 5000     # time steps of the full design gradient (the workload's horizon)
-NSNAP = 64             # checkpoint slots in device memory
+# Checkpoint slots in device memory, chosen from the HBM budget: 128 FP32
+# states of 319 MB = 41 GB (the recomputation falls from 8906 steps at 64 slots
+# to 4873; more slots gain little: 4745 at 256).
+NSNAP = 128
 METRIC = "MLUPS fwd+adjoint D3Q19"
 CONFIG_NAME = ("D3Q19 MRT (d'Humieres, s_nu from tau=0.6, other rates 1.2) + Brinkman "
                "partial bounce-back duct 256x128x128, Hecht velocity inlet u_max=0.04, "
@@ -406,8 +409,9 @@ def main():
     e2e = {"value": round(e2e_value, 2), "unit": "MLUPS",
            "h2d_bytes_per_step": int(cells * 8), "d2h_bytes_per_step": int(cells * 8 + 8),
            "what": "lbm_set_design (host FP64 design) + lbm_gradient (5000 forward steps, "
-                   "%d recomputed by Wang checkpointing in 64 device slots, 5000 adjoint "
-                   "steps) + dJ/dgamma to host, per step" % recomputed,
+                   "%d recomputed by Wang checkpointing in %d device slots (%.0f GB), 5000 adjoint "
+                   "steps) + dJ/dgamma to host, per step" % (recomputed, NSNAP,
+                                                             NSNAP * cells * 19 * 4 / 1e9),
            "gradient_s": round(grad_fp32_s, 4),
            "forward_sweep_ms": round(float(st.forward_ms), 2),
            "reverse_sweep_ms": round(float(st.reverse_ms), 2)}
