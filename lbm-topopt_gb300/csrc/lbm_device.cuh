@@ -999,13 +999,20 @@ struct Dither {
   unsigned r;
   // key: step_key(step, salt), the same for every cell of a launch
   __device__ __forceinline__ Dither(unsigned cell, unsigned key) : r(mix32(cell ^ key)) {}
+  // uniform in [1, 2) * 2^-K, 23 random mantissa bits (the sequence's low
+  // bits have short periods, but they weigh below 2^-16 of the variate, and
+  // over the cells' seeds every bit is uniform, so the rounding stays unbiased)
+  template <int K>
+  __device__ __forceinline__ float raw() {
+    r = r * 1664525u + 1013904223u;
+    constexpr unsigned kExp = (unsigned)(127 - K) << 23;
+    return __uint_as_float(kExp | (r & 0x7fffffu));
+  }
   // uniform in [-1/2, 1/2) * 2^-K for K = 23 (FP32) or 10 (FP16)
   template <int K>
   __device__ __forceinline__ float next() {
-    r = r * 1664525u + 1013904223u;
-    constexpr unsigned kExp = (unsigned)(127 - K) << 23;
     constexpr float kHalf = 1.5f / (float)(1u << K);
-    return __uint_as_float(kExp | (r >> 9)) - kHalf;
+    return raw<K>() - kHalf;
   }
 };
 
@@ -1031,6 +1038,22 @@ struct Round<float> {
   __device__ static __forceinline__ float apply(float f, float d, Dither& rnd) {
     return f + fmaf(rnd.next<23>(), pow2_floor(f), d);
   }
+  // two populations at once (packed FP32x2 arithmetic where the GPU has it)
+  __device__ static __forceinline__ void apply_pair(float fa, float fb, float da, float db,
+                                                    Dither& rnd, float& oa, float& ob) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    constexpr float kHalf = 1.5f / (float)(1u << 23);
+    const float ua = rnd.raw<23>(), ub = rnd.raw<23>();
+    const float2 u = __fadd2_rn(make_float2(ua, ub), make_float2(-kHalf, -kHalf));
+    const float2 n = __ffma2_rn(u, make_float2(pow2_floor(fa), pow2_floor(fb)), make_float2(da, db));
+    const float2 o = __fadd2_rn(make_float2(fa, fb), n);
+    oa = o.x;
+    ob = o.y;
+#else
+    oa = apply(fa, da, rnd);
+    ob = apply(fb, db, rnd);
+#endif
+  }
 };
 template <>
 struct Round<__half> {
@@ -1040,7 +1063,29 @@ struct Round<__half> {
     const float bin = fmaxf(pow2_floor(s), 6.103515625e-05f);
     return __float2half_rn(fmaf(rnd.next<10>(), bin, s));
   }
+  __device__ static __forceinline__ void apply_pair(float fa, float fb, float da, float db,
+                                                    Dither& rnd, __half& oa, __half& ob) {
+    oa = apply(fa, da, rnd);
+    ob = apply(fb, db, rnd);
+  }
 };
+
+// (0.5 (e + a), 0.5 (e - a)): the increments of a population pair from its
+// even and odd parts
+__device__ __forceinline__ void pair_halves(float e, float a, float& p, float& m) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  const float2 v = __fmul2_rn(make_float2(0.5f, 0.5f), __fadd2_rn(make_float2(e, e), make_float2(a, -a)));
+  p = v.x;
+  m = v.y;
+#else
+  p = 0.5f * (e + a);
+  m = 0.5f * (e - a);
+#endif
+}
+__device__ __forceinline__ void pair_halves(double e, double a, double& p, double& m) {
+  p = 0.5 * (e + a);
+  m = 0.5 * (e - a);
+}
 
 // sum_a e_ia j_a with the zero terms left out
 template <int LAT, int i, class C>
@@ -1080,9 +1125,10 @@ __device__ __forceinline__ void project_conserved(C* d) {
 
 // Increments of mrt3d_pair_collide (same operator: f + d is its output),
 // handed to emit(q, d_q) pair by pair so each pair's registers are freed early.
-template <class C, class Emit>
+template <class C, class Emit, class Emit2>
 __device__ __forceinline__ void mrt3d_pair_collide_inc(const C* f, C imult, C& rho, C& jx, C& jy,
-                                                       C& jz, const KParams& p, Emit&& emit) {
+                                                       C& jz, const KParams& p, Emit&& emit,
+                                                       Emit2&& emit2) {
   C s[10], a[10], mo[15];
   mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, mo);
   mrt3d_relax(mo, rho, jx, jy, jz, p);
@@ -1114,19 +1160,20 @@ __device__ __forceinline__ void mrt3d_pair_collide_inc(const C* f, C imult, C& r
     // s' = s + E, a'' = (a + O)(1 - 2 imult) = a + O - 2 imult (a + O); a is
     // recomputed from f (same value) so that only f stays live across the loop
     const C da = O - twoim * ((f[d] - f[d + 9]) + O);
-    emit(std::integral_constant<int, d>{}, C(0.5) * (E + da));
-    emit(std::integral_constant<int, d + 9>{}, C(0.5) * (E - da));
+    C dp, dm;
+    pair_halves(E, da, dp, dm);
+    emit2(std::integral_constant<int, d>{}, std::integral_constant<int, d + 9>{}, dp, dm);
   });
 }
 
 // Increments of flow_collide (collision + partial bounce-back), handed to
 // emit(q, d_q) once per flow population; returns the macros of the input.
-template <int LAT, int COLL, class C, class Emit>
+template <int LAT, int COLL, class C, class Emit, class Emit2>
 __device__ __forceinline__ void flow_collide_inc(const C* f, C imult, C& rho, C& jx, C& jy, C& jz,
-                                                 const KParams& p, Emit&& emit) {
+                                                 const KParams& p, Emit&& emit, Emit2&& emit2) {
   using L = Lattice<LAT>;
   if constexpr (LAT == LAT_D3Q19 && COLL == LBM_MRT) {
-    mrt3d_pair_collide_inc(f, imult, rho, jx, jy, jz, p, emit);
+    mrt3d_pair_collide_inc(f, imult, rho, jx, jy, jz, p, emit, emit2);
   } else {
     C d[L::QF];
     flow_macros<LAT>(f, rho, jx, jy, jz);
@@ -1169,8 +1216,8 @@ __device__ __forceinline__ void flow_collide_inc(const C* f, C imult, C& rho, C&
     static_for<L::HALF>([&](auto D) {
       constexpr int k = decltype(D)::value + 1;
       const C m = imult * ((f[k + L::HALF] - f[k]) + (d[k + L::HALF] - d[k]));
-      emit(std::integral_constant<int, k>{}, d[k] + m);
-      emit(std::integral_constant<int, k + L::HALF>{}, d[k + L::HALF] - m);
+      emit2(std::integral_constant<int, k>{}, std::integral_constant<int, k + L::HALF>{}, d[k] + m,
+            d[k + L::HALF] - m);
     });
   }
 }

@@ -190,10 +190,16 @@ __device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, i
       // FP32/FP16 storage: increments, rounded to the storage type without bias
       Dither rnd((unsigned)c, p.key_fwd);
       S o[L::Q];
-      flow_collide_inc<LAT, COLL>(f, imult, rho, jx, jy, jz, p, [&](auto Q_, C dq) {
-        constexpr int q = decltype(Q_)::value;
-        o[q] = Round<S>::apply(f[q], dq, rnd);
-      });
+      flow_collide_inc<LAT, COLL>(
+          f, imult, rho, jx, jy, jz, p,
+          [&](auto Q_, C dq) {
+            constexpr int q = decltype(Q_)::value;
+            o[q] = Round<S>::apply(f[q], dq, rnd);
+          },
+          [&](auto QA_, auto QB_, C da, C db) {
+            constexpr int qa = decltype(QA_)::value, qb = decltype(QB_)::value;
+            Round<S>::apply_pair(f[qa], f[qb], da, db, rnd, o[qa], o[qb]);
+          });
       if constexpr (LAT == LAT_D2Q9_D2Q5)
         thermal_collide_inc(f + 9, jx, jy, g, p, [&](auto I_, C dq) {
           constexpr int q = decltype(I_)::value + 9;

@@ -111,9 +111,12 @@ void collide_inc(const lbm_config* cfg, const double* fin, double g, double* fou
   const C gg = (C)g;
   const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(gg, mp<C>(p).pbb_q));
   C rho, jx, jy, jz;
-  flow_collide_inc<LAT, COLL>(f, imult, rho, jx, jy, jz, p, [&](auto Q_, C dq) {
-    d[decltype(Q_)::value] = dq;
-  });
+  flow_collide_inc<LAT, COLL>(
+      f, imult, rho, jx, jy, jz, p, [&](auto Q_, C dq) { d[decltype(Q_)::value] = dq; },
+      [&](auto QA_, auto QB_, C da, C db) {
+        d[decltype(QA_)::value] = da;
+        d[decltype(QB_)::value] = db;
+      });
   if constexpr (LAT == LAT_D2Q9_D2Q5)
     thermal_collide_inc(f + 9, jx, jy, gg, p, [&](auto I_, C dq) { d[decltype(I_)::value + 9] = dq; });
   for (int i = 0; i < Q; ++i) fout[i] = (double)f[i] + (double)d[i];
