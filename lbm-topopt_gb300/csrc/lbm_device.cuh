@@ -483,50 +483,147 @@ static_assert(mrt3d_even(0) && mrt3d_even(1) && mrt3d_odd(2) && mrt3d_odd(3) && 
 
 // d(meq_k)/d(rho) and d(meq_k)/d(j_a) of MRT3d.hh:92-109 are applied inline below.
 
+// rho, j and the 15 moment rows of the populations (f0, s_d, a_d) in pair form.
+template <class C>
+__device__ __forceinline__ void mrt3d_pair_rows(C f0, const C* s, const C* a, C& rho, C& jx, C& jy,
+                                                C& jz, C* mo) {
+  using L = Lattice<LAT_D3Q19>;
+  // The rows share sub-sums (pair d: 1-3 the z, y, x axes, 4-5 the yz, 6-7
+  // the xz and 8-9 the xy diagonals); the identities are checked row by row
+  // against the moment table by tests/device_math_host.cpp.
+  static_assert(L::ez(1) == -1 && L::ey(2) == -1 && L::ex(3) == -1 && L::ey(4) == -1 &&
+                    L::ez(4) == -1 && L::ey(5) == 1 && L::ex(6) == -1 && L::ex(7) == 1 &&
+                    L::ey(8) == -1 && L::ex(9) == 1 && L::ey(9) == -1,
+                "pair order of the factored D3Q19 moments");
+  // even rows: e, eps, 3pxx, 3pixx, pww, piww, pxy, pyz, pxz
+  const C sax = (s[1] + s[2]) + s[3];
+  const C dyz = s[4] + s[5], dxz = s[6] + s[7], dxy = s[8] + s[9];
+  const C sdg = (dyz + dxz) + dxy;
+  rho = (f0 + sax) + sdg;
+  mo[0] = C(8.) * sdg - (C(30.) * f0 + C(11.) * sax);
+  mo[1] = (C(12.) * f0 + sdg) - C(4.) * sax;
+  const C A = C(2.) * s[3] - (s[1] + s[2]), B = (dxz + dxy) - C(2.) * dyz;
+  mo[5] = A + B;
+  mo[6] = B - C(2.) * A;
+  const C A2 = s[2] - s[1], B2 = dxy - dxz;
+  mo[7] = A2 + B2;
+  mo[8] = B2 - C(2.) * A2;
+  mo[9] = s[8] - s[9];
+  mo[10] = s[4] - s[5];
+  mo[11] = s[6] - s[7];
+  // odd rows: j and q (x, y, z), m (x, y, z)
+  const C ux = a[9] - a[8], vx = a[7] - a[6], X = ux + vx;
+  jx = X - a[3];
+  mo[2] = X + C(4.) * a[3];
+  mo[12] = ux - vx;
+  const C py = a[5] - a[4], qy = a[8] + a[9], Y = py - qy;
+  jy = Y - a[2];
+  mo[3] = Y + C(4.) * a[2];
+  mo[13] = py + qy;
+  const C rz = a[4] + a[5], tz = a[6] + a[7], Z = rz + tz;
+  jz = -(Z + a[1]);
+  mo[4] = C(4.) * a[1] - Z;
+  mo[14] = rz - tz;
+}
+
 template <class C>
 __device__ __forceinline__ void mrt3d_pair_moments(const C* f, C* s, C* a, C& rho, C& jx, C& jy,
                                                    C& jz, C* mo) {
-  using L = Lattice<LAT_D3Q19>;
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
     s[d] = f[d] + f[d + 9];
     a[d] = f[d] - f[d + 9];
   });
-  rho = f[0];
-  jx = C(0.);
-  jy = C(0.);
-  jz = C(0.);
-  static_for<9>([&](auto D) {
-    constexpr int d = decltype(D)::value + 1;
-    rho += s[d];
-    if constexpr (L::ex(d) == 1) jx += a[d];
-    if constexpr (L::ex(d) == -1) jx -= a[d];
-    if constexpr (L::ey(d) == 1) jy += a[d];
-    if constexpr (L::ey(d) == -1) jy -= a[d];
-    if constexpr (L::ez(d) == 1) jz += a[d];
-    if constexpr (L::ez(d) == -1) jz -= a[d];
-  });
+  mrt3d_pair_rows(f[0], s, a, rho, jx, jy, jz, mo);
+}
+
+// Even part of the back-map of the relaxed moments r (mo after mrt3d_relax):
+// d0 = -sum_k (M[k][0]/N_k) r_k for the rest population and
+// E_d = -2 sum_even k (M[k][d]/N_k) r_k for pair d, from nine shared terms.
+template <class C>
+struct Mrt3dEvenBack {
+  C d0, ax12, R, e3, c45, h10, c67, h11, c89, h9;
+  __device__ __forceinline__ explicit Mrt3dEvenBack(const C* mo) {
+    d0 = C(30. / 2394.) * mo[0] - C(12. / 252.) * mo[1];
+    const C cax = C(22. / 2394.) * mo[0] + C(8. / 252.) * mo[1];
+    const C cdg = C(-16. / 2394.) * mo[0] - C(2. / 252.) * mo[1];
+    const C P = C(1. / 18.) * (mo[5] - mo[6]);
+    const C Q = C(1. / 18.) * mo[5] + C(1. / 36.) * mo[6];
+    R = C(1. / 6.) * (mo[7] - mo[8]);
+    const C T = C(1. / 6.) * mo[7] + C(1. / 12.) * mo[8];
+    ax12 = cax + P;
+    e3 = cax - C(2.) * P;
+    c45 = cdg + C(2.) * Q;
+    const C cq = cdg - Q;
+    c67 = cq + T;
+    c89 = cq - T;
+    h9 = C(0.5) * mo[9];
+    h10 = C(0.5) * mo[10];
+    h11 = C(0.5) * mo[11];
+  }
+  template <int d>
+  __device__ __forceinline__ C E() const {
+    if constexpr (d == 1) return ax12 + R;
+    if constexpr (d == 2) return ax12 - R;
+    if constexpr (d == 3) return e3;
+    if constexpr (d == 4) return c45 - h10;
+    if constexpr (d == 5) return c45 + h10;
+    if constexpr (d == 6) return c67 - h11;
+    if constexpr (d == 7) return c67 + h11;
+    if constexpr (d == 8) return c89 - h9;
+    if constexpr (d == 9) return c89 + h9;
+  }
+};
+
+// Transpose of the even rows: G_0 = sum_k M[k][0] m_k and, for pair d,
+// G_d = sum_even k M[k][d] m_k (the same sub-sums as Mrt3dEvenBack).
+template <class C>
+struct Mrt3dEvenRowsT {
+  C g0, ax12, R, g3, c45, m10, c67, m11, c89, m9;
+  __device__ __forceinline__ explicit Mrt3dEvenRowsT(const C* m) {
+    g0 = C(12.) * m[1] - C(30.) * m[0];
+    const C cax = C(-11.) * m[0] - C(4.) * m[1];
+    const C cdg = C(8.) * m[0] + m[1];
+    const C P = m[5] - C(2.) * m[6], Q = m[5] + m[6];
+    R = m[7] - C(2.) * m[8];
+    const C T = m[7] + m[8];
+    ax12 = cax - P;
+    g3 = cax + C(2.) * P;
+    c45 = cdg - C(2.) * Q;
+    const C cq = cdg + Q;
+    c67 = cq - T;
+    c89 = cq + T;
+    m9 = m[9];
+    m10 = m[10];
+    m11 = m[11];
+  }
+  template <int d>
+  __device__ __forceinline__ C G() const {
+    if constexpr (d == 1) return ax12 - R;
+    if constexpr (d == 2) return ax12 + R;
+    if constexpr (d == 3) return g3;
+    if constexpr (d == 4) return c45 + m10;
+    if constexpr (d == 5) return c45 - m10;
+    if constexpr (d == 6) return c67 + m11;
+    if constexpr (d == 7) return c67 - m11;
+    if constexpr (d == 8) return c89 + m9;
+    if constexpr (d == 9) return c89 - m9;
+  }
+};
+
+// Odd part of the back-map: O_d = -2 sum_odd k (M[k][d]/N_k) r_k.
+template <int d, class C>
+__device__ __forceinline__ C mrt3d_odd_back(const C* mo) {
+  C O = C(0.);
   static_for<15>([&](auto KK) {
     constexpr int k = decltype(KK)::value;
-    C acc = C(0.);
-    if constexpr (mrt3d_even(k)) {
-      constexpr int c0 = mrt3d_m(k, 0);
-      if constexpr (c0 != 0) acc = C(c0) * f[0];
+    constexpr int c = mrt3d_m(k, d);
+    if constexpr (mrt3d_odd(k) && c != 0) {
+      constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
+      O += C(b) * mo[k];
     }
-    static_for<9>([&](auto D) {
-      constexpr int d = decltype(D)::value + 1;
-      constexpr int c = mrt3d_m(k, d);
-      const C v = mrt3d_even(k) ? s[d] : a[d];
-      if constexpr (c == 1) {
-        acc += v;
-      } else if constexpr (c == -1) {
-        acc -= v;
-      } else if constexpr (c != 0) {
-        acc += C(c) * v;
-      }
-    });
-    mo[k] = acc;
   });
+  return O;
 }
 
 // In place: f <- PBB(MRT(f)); returns the macros of the input.
@@ -537,33 +634,13 @@ __device__ __forceinline__ void mrt3d_pair_collide(C* f, C imult, C& rho, C& jx,
   mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, mo);
   mrt3d_relax(mo, rho, jx, jy, jz, p);
   // rest population: f_0 - sum_even (M[k][0]/N_k) r_k
-  C f0 = f[0];
-  static_for<15>([&](auto KK) {
-    constexpr int k = decltype(KK)::value;
-    constexpr int c = mrt3d_m(k, 0);
-    if constexpr (mrt3d_even(k) && c != 0) {
-      constexpr double b = -(double)c / (double)mrt3d_n(k);
-      f0 += C(b) * mo[k];
-    }
-  });
-  f[0] = f0;
+  const Mrt3dEvenBack<C> eb(mo);
+  f[0] += eb.d0;
   const C keep = C(1.) - C(2.) * imult;
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
-    C E = C(0.), O = C(0.);
-    static_for<15>([&](auto KK) {
-      constexpr int k = decltype(KK)::value;
-      constexpr int c = mrt3d_m(k, d);
-      if constexpr (c != 0) {
-        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
-        if constexpr (mrt3d_even(k))
-          E += C(b) * mo[k];
-        else
-          O += C(b) * mo[k];
-      }
-    });
-    const C sp = s[d] + E;
-    const C ap = (a[d] + O) * keep;
+    const C sp = s[d] + eb.template E<d>();
+    const C ap = (a[d] + mrt3d_odd_back<d>(mo)) * keep;
     f[d] = C(0.5) * (sp + ap);
     f[d + 9] = C(0.5) * (sp - ap);
   });
@@ -578,51 +655,32 @@ __device__ __forceinline__ void mrt3d_pair_reverse(const C* fin, C* lam, C imult
   C rho, jx, jy, jz;
   mrt3d_pair_moments(fin, s, a, rho, jx, jy, jz, mo);
   mrt3d_relax(mo, rho, jx, jy, jz, p);
-  // adjoints of s' and a'' from the output pairs; imult adjoint from a' = a + 2 O
+  // adjoints of s' and a'' from the output pairs, kept doubled:
+  // ls_d = 2 sbar'_d, la_d = 2 abar'_d; imult adjoint from a' = a + O
   const C keep = C(1.) - C(2.) * imult;
-  C sb[10], ab[10];
+  C ls[10], la[10];
   C imultRev = C(0.);
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
-    C O = C(0.);
-    static_for<15>([&](auto KK) {
-      constexpr int k = decltype(KK)::value;
-      constexpr int c = mrt3d_m(k, d);
-      if constexpr (c != 0 && !mrt3d_even(k)) {
-        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
-        O += C(b) * mo[k];
-      }
-    });
-    const C ap = a[d] + O;                      // a' before partial bounce-back
-    sb[d] = C(0.5) * (lam[d] + lam[d + 9]);      // adjoint of s'
-    const C ab2 = C(0.5) * (lam[d] - lam[d + 9]);  // adjoint of a''
-    imultRev -= C(2.) * ap * ab2;
-    ab[d] = keep * ab2;                          // adjoint of a'
+    const C ap = a[d] + mrt3d_odd_back<d>(mo);  // a' before partial bounce-back
+    ls[d] = lam[d] + lam[d + 9];
+    const C la2 = lam[d] - lam[d + 9];          // 2 x adjoint of a''
+    imultRev -= ap * la2;
+    la[d] = keep * la2;
   });
   dg += dimult * imultRev;
   const C f0b = lam[0];
-  // adjoint of the relaxed moments, then of (m_k - meq_k)
+  // adjoint of the relaxed moments: mb_k = rate_k (-1/N_k) (M lam)_k, the
+  // rows applied to (f0b, ls, la) in pair form
+  C mb[15];
+  {
+    C r_, x_, y_, z_;
+    mrt3d_pair_rows(f0b, ls, la, r_, x_, y_, z_, mb);
+  }
   const C* rt = mp<C>(p).mrt;
   const C om = mp<C>(p).omega;
-  C mb[15];
   static_for<15>([&](auto KK) {
     constexpr int k = decltype(KK)::value;
-    C acc = C(0.);
-    if constexpr (mrt3d_even(k)) {
-      constexpr int c0 = mrt3d_m(k, 0);
-      if constexpr (c0 != 0) {
-        constexpr double b0 = -(double)c0 / (double)mrt3d_n(k);
-        acc += C(b0) * f0b;
-      }
-    }
-    static_for<9>([&](auto D) {
-      constexpr int d = decltype(D)::value + 1;
-      constexpr int c = mrt3d_m(k, d);
-      if constexpr (c != 0) {
-        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
-        acc += C(b) * (mrt3d_even(k) ? sb[d] : ab[d]);
-      }
-    });
     // rate of moment k (MRT3d.hh:93-109)
     C rate;
     if constexpr (k == 0) rate = rt[0];
@@ -631,7 +689,7 @@ __device__ __forceinline__ void mrt3d_pair_reverse(const C* fin, C* lam, C imult
     else if constexpr (k == 6 || k == 8) rate = rt[3];
     else if constexpr (k >= 12) rate = rt[4];
     else rate = om;
-    mb[k] = rate * acc;
+    mb[k] = rate * (C(-1.0 / (double)mrt3d_n(k)) * mb[k]);
   });
   // through -meq(rho, j)
   const C we = rt[5], wej = rt[6], wxx = rt[7];
@@ -645,27 +703,17 @@ __device__ __forceinline__ void mrt3d_pair_reverse(const C* fin, C* lam, C imult
   const C jR2 = -(mb[0] * C(38.) * jz + mb[1] * C(2.) * wej * jz + mb[4] * c2 - a56 * C(2.) * jz -
                   a78 * C(2.) * jz + mb[10] * jy + mb[11] * jx);
   // through m = M(f0, s, a), rho = f0 + sum s, j = sum e a, and the pair split
-  C f0bar = f0b + rR;
-  static_for<15>([&](auto KK) {
-    constexpr int k = decltype(KK)::value;
-    constexpr int c0 = mrt3d_m(k, 0);
-    if constexpr (mrt3d_even(k) && c0 != 0) f0bar += C(c0) * mb[k];
-  });
-  lam[0] = f0bar;
+  const Mrt3dEvenRowsT<C> gt(mb);
+  lam[0] = (f0b + rR) + gt.g0;
   using L = Lattice<LAT_D3Q19>;
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
-    C sbar = sb[d] + rR;
-    C abar = ab[d] + (jR0 * C(L::ex(d)) + jR1 * C(L::ey(d)) + jR2 * C(L::ez(d)));
+    const C sbar = (C(0.5) * ls[d] + rR) + gt.template G<d>();
+    C abar = C(0.5) * la[d] + (jR0 * C(L::ex(d)) + jR1 * C(L::ey(d)) + jR2 * C(L::ez(d)));
     static_for<15>([&](auto KK) {
       constexpr int k = decltype(KK)::value;
       constexpr int c = mrt3d_m(k, d);
-      if constexpr (c != 0) {
-        if constexpr (mrt3d_even(k))
-          sbar += C(c) * mb[k];
-        else
-          abar += C(c) * mb[k];
-      }
+      if constexpr (c != 0 && mrt3d_odd(k)) abar += C(c) * mb[k];
     });
     lam[d] = sbar + abar;
     lam[d + 9] = sbar - abar;
@@ -1132,31 +1180,13 @@ __device__ __forceinline__ void mrt3d_pair_collide_inc(const C* f, C imult, C& r
   C s[10], a[10], mo[15];
   mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, mo);
   mrt3d_relax(mo, rho, jx, jy, jz, p);
-  C d0 = C(0.);
-  static_for<15>([&](auto KK) {
-    constexpr int k = decltype(KK)::value;
-    constexpr int c = mrt3d_m(k, 0);
-    if constexpr (mrt3d_even(k) && c != 0) {
-      constexpr double b = -(double)c / (double)mrt3d_n(k);
-      d0 += C(b) * mo[k];
-    }
-  });
-  emit(std::integral_constant<int, 0>{}, d0);
+  const Mrt3dEvenBack<C> eb(mo);
+  emit(std::integral_constant<int, 0>{}, eb.d0);
   const C twoim = C(2.) * imult;
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
-    C E = C(0.), O = C(0.);
-    static_for<15>([&](auto KK) {
-      constexpr int k = decltype(KK)::value;
-      constexpr int c = mrt3d_m(k, d);
-      if constexpr (c != 0) {
-        constexpr double b = -2.0 * (double)c / (double)mrt3d_n(k);
-        if constexpr (mrt3d_even(k))
-          E += C(b) * mo[k];
-        else
-          O += C(b) * mo[k];
-      }
-    });
+    const C E = eb.template E<d>();
+    const C O = mrt3d_odd_back<d>(mo);
     // s' = s + E, a'' = (a + O)(1 - 2 imult) = a + O - 2 imult (a + O); a is
     // recomputed from f (same value) so that only f stays live across the loop
     const C da = O - twoim * ((f[d] - f[d + 9]) + O);

@@ -225,6 +225,46 @@ void dev_round(int half, float f, float d, int n, unsigned step, double* out) {
                   : (double)Round<float>::apply(f, d, rnd);
   }
 }
+// The D3Q19 moment table (15 x 19 rows M, norms N) and the factored pair
+// forms computed from it: dev_mrt3d_moments gives rho, jx, jy, jz and the 15
+// rows of f; dev_mrt3d_back gives, for relaxed moments r, d0 then E_d and O_d
+// for d = 1..9 (19 values).
+void dev_mrt3d_table(int* M, int* N) {
+  for (int k = 0; k < 15; ++k) {
+    N[k] = mrt3d_n(k);
+    for (int i = 0; i < 19; ++i) M[k * 19 + i] = mrt3d_m(k, i);
+  }
+}
+void dev_mrt3d_moments(const double* f, double* out) {
+  double s[10], a[10], rho, jx, jy, jz;
+  for (int d = 1; d <= 9; ++d) {
+    s[d] = f[d] + f[d + 9];
+    a[d] = f[d] - f[d + 9];
+  }
+  mrt3d_pair_moments(f, s, a, rho, jx, jy, jz, out + 4);
+  out[0] = rho;
+  out[1] = jx;
+  out[2] = jy;
+  out[3] = jz;
+}
+void dev_mrt3d_back(const double* r, double* out) {
+  const Mrt3dEvenBack<double> eb(r);
+  out[0] = eb.d0;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    out[d] = eb.template E<d>();
+    out[d + 9] = mrt3d_odd_back<d>(r);
+  });
+}
+// Transposed even rows for moment adjoints m: G_0, then G_d for d = 1..9.
+void dev_mrt3d_rows_t(const double* m, double* out) {
+  const Mrt3dEvenRowsT<double> gt(m);
+  out[0] = gt.g0;
+  static_for<9>([&](auto D) {
+    constexpr int d = decltype(D)::value + 1;
+    out[d] = gt.template G<d>();
+  });
+}
 int dev_collide(const lbm_config* c, int fp32, const double* fin, double g, double* fout) {
   return fp32 ? dispatch_collide<float>(c, fin, g, fout) : dispatch_collide<double>(c, fin, g, fout);
 }

@@ -48,6 +48,15 @@ def devmath():
     lib.dev_reverse_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
     lib.dev_round.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round.restype = None
+    ip = C.POINTER(C.c_int)
+    lib.dev_mrt3d_table.argtypes = [ip, ip]
+    lib.dev_mrt3d_table.restype = None
+    lib.dev_mrt3d_moments.argtypes = [dp, dp]
+    lib.dev_mrt3d_moments.restype = None
+    lib.dev_mrt3d_back.argtypes = [dp, dp]
+    lib.dev_mrt3d_back.restype = None
+    lib.dev_mrt3d_rows_t.argtypes = [dp, dp]
+    lib.dev_mrt3d_rows_t.restype = None
     return lib
 
 
@@ -174,3 +183,39 @@ def test_stochastic_rounding_is_unbiased(devmath, half):
         x = float(np.float32(f)) + float(np.float32(d))
         ulp_lo = float(np.spacing(dt(min(abs(x), f) * 0.999)))
         assert abs(out.mean() - x) < 0.25 * ulp_lo, (f, d, (out.mean() - x) / ulp_lo)
+
+
+def test_factored_d3q19_moments_match_the_table(devmath):
+    """The pair-form D3Q19 moments and back-map are written with shared
+    sub-sums; row by row they must equal the moment table (MRT3d.hh:50-90):
+    m = M f, the back-map -M^T diag(1/N) r split into the rest population,
+    the pair sums (twice the even part) and differences, and the transposed
+    even rows M_even^T m of the adjoint."""
+    ip = C.POINTER(C.c_int)
+    dp = C.POINTER(C.c_double)
+    M = np.zeros((15, 19), dtype=np.int32)
+    N = np.zeros(15, dtype=np.int32)
+    devmath.dev_mrt3d_table(M.ctypes.data_as(ip), N.ctypes.data_as(ip))
+    ex = np.array([0, 0, 0, -1, 0, 0, -1, 1, -1, 1, 0, 0, 1, 0, 0, 1, -1, 1, -1])
+    ey = np.array([0, 0, -1, 0, -1, 1, 0, 0, -1, -1, 0, 1, 0, 1, -1, 0, 0, 1, 1])
+    ez = np.array([0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 1, 0, 0, 1, 1, 1, 1, 0, 0])
+    full = np.vstack([np.ones(19), ex, ey, ez, M]).astype(float)
+    assert np.linalg.matrix_rank(full) == 19
+    rng = np.random.default_rng(5)
+    out = np.zeros(19)
+    for _ in range(10):
+        f = rng.standard_normal(19)
+        devmath.dev_mrt3d_moments(f.ctypes.data_as(dp), out.ctypes.data_as(dp))
+        assert np.abs(out - full @ f).max() < 1e-13
+        r = rng.standard_normal(15)
+        devmath.dev_mrt3d_back(r.ctypes.data_as(dp), out.ctypes.data_as(dp))
+        back = -(M.T.astype(float) / N) @ r
+        assert abs(out[0] - back[0]) < 1e-14
+        assert np.abs(out[1:10] - (back[1:10] + back[10:19])).max() < 1e-14
+        assert np.abs(out[10:19] - (back[1:10] - back[10:19])).max() < 1e-14
+        m = rng.standard_normal(15)
+        even = np.array([np.all(M[k, 1:10] == M[k, 10:19]) for k in range(15)])
+        devmath.dev_mrt3d_rows_t(m.ctypes.data_as(dp), out.ctypes.data_as(dp))
+        gt = M[even].T.astype(float) @ m[even]
+        assert abs(out[0] - gt[0]) < 1e-13
+        assert np.abs(out[1:10] - gt[1:10]).max() < 1e-13
