@@ -260,13 +260,24 @@ __host__ __device__ inline bool in_box(const int* b, int x, int y, int z) {
 // ---------------------------------------------------------------------------
 // Interpolations (core/interpolationFunctions.hh:17-54).
 
+// a / b; FP32 on the GPU takes the fast division (about 2 units in the last
+// place for the denominators here, q + s in [q, q + 1]), FP64 stays exact.
+template <class C>
+__device__ __forceinline__ C interp_div(C a, C b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(C) == 4) return __fdividef(a, b);
+#endif
+  return a / b;
+}
+
 template <class C>
 __device__ __forceinline__ C bp(C s, C q) {
-  return C(1.) - s * (C(1.) + q) / (q + s);
+  return C(1.) - interp_div(s * (C(1.) + q), q + s);
 }
 template <class C>
 __device__ __forceinline__ C bp_diff(C s, C q) {
-  return (-(C(1.) + q) / (q + s) + s * (C(1.) + q) / ((q + s) * (q + s)));
+  const C r = interp_div(C(1.), q + s);
+  return (C(1.) + q) * r * (s * r - C(1.));
 }
 template <class C>
 __device__ __forceinline__ C ramp(C s, C q, C ck) {
@@ -1042,7 +1053,7 @@ __host__ __device__ __forceinline__ unsigned mix32(unsigned v) {
 }
 
 // Per-cell stream of uniform variates: a hash of (cell, step, salt) seeds a
-// 32-bit linear congruential sequence whose top 23 bits are used.
+// 32-bit linear congruential sequence; each draw gives one or two variates.
 struct Dither {
   unsigned r;
   // key: step_key(step, salt), the same for every cell of a launch
@@ -1061,6 +1072,17 @@ struct Dither {
   __device__ __forceinline__ float next() {
     constexpr float kHalf = 1.5f / (float)(1u << K);
     return raw<K>() - kHalf;
+  }
+  // Two variates of raw<K>() from one draw: a from bits 0-22, b from bits
+  // 9-31.  Each is uniform on its own; they share bits 9-22, which are a's
+  // leading bits but only b's trailing ones (below 2^-9 of b), so b's
+  // leading nine bits (23-31) are independent of a.
+  template <int K>
+  __device__ __forceinline__ void raw_pair(float& a, float& b) {
+    r = r * 1664525u + 1013904223u;
+    constexpr unsigned kExp = (unsigned)(127 - K) << 23;
+    a = __uint_as_float(kExp | (r & 0x7fffffu));
+    b = __uint_as_float(kExp | (r >> 9));
   }
 };
 
@@ -1086,20 +1108,22 @@ struct Round<float> {
   __device__ static __forceinline__ float apply(float f, float d, Dither& rnd) {
     return f + fmaf(rnd.next<23>(), pow2_floor(f), d);
   }
-  // two populations at once (packed FP32x2 arithmetic where the GPU has it)
+  // Two populations at once from one draw (Dither::raw_pair), in packed
+  // FP32x2 arithmetic where the GPU has it; the same values either way.
   __device__ static __forceinline__ void apply_pair(float fa, float fb, float da, float db,
                                                     Dither& rnd, float& oa, float& ob) {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
     constexpr float kHalf = 1.5f / (float)(1u << 23);
-    const float ua = rnd.raw<23>(), ub = rnd.raw<23>();
+    float ua, ub;
+    rnd.raw_pair<23>(ua, ub);
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
     const float2 u = __fadd2_rn(make_float2(ua, ub), make_float2(-kHalf, -kHalf));
     const float2 n = __ffma2_rn(u, make_float2(pow2_floor(fa), pow2_floor(fb)), make_float2(da, db));
     const float2 o = __fadd2_rn(make_float2(fa, fb), n);
     oa = o.x;
     ob = o.y;
 #else
-    oa = apply(fa, da, rnd);
-    ob = apply(fb, db, rnd);
+    oa = fa + fmaf(ua - kHalf, pow2_floor(fa), da);
+    ob = fb + fmaf(ub - kHalf, pow2_floor(fb), db);
 #endif
   }
 };

@@ -265,6 +265,18 @@ void dev_mrt3d_rows_t(const double* m, double* out) {
     out[d] = gt.template G<d>();
   });
 }
+// Round<float>::apply_pair of (f, d) twice per cell for n cells: out[2i] and
+// out[2i+1] are the two stored values of cell i.
+void dev_round_pair(float f, float d, int n, unsigned step, double* out) {
+  const unsigned key = step_key(step, kSaltForward);
+  for (int i = 0; i < n; ++i) {
+    Dither rnd((unsigned)i, key);
+    float a, b;
+    Round<float>::apply_pair(f, f, d, d, rnd, a, b);
+    out[2 * i] = (double)a;
+    out[2 * i + 1] = (double)b;
+  }
+}
 int dev_collide(const lbm_config* c, int fp32, const double* fin, double g, double* fout) {
   return fp32 ? dispatch_collide<float>(c, fin, g, fout) : dispatch_collide<double>(c, fin, g, fout);
 }

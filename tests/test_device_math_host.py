@@ -48,6 +48,8 @@ def devmath():
     lib.dev_reverse_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
     lib.dev_round.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round.restype = None
+    lib.dev_round_pair.argtypes = [C.c_float, C.c_float, C.c_int, C.c_uint, dp]
+    lib.dev_round_pair.restype = None
     ip = C.POINTER(C.c_int)
     lib.dev_mrt3d_table.argtypes = [ip, ip]
     lib.dev_mrt3d_table.restype = None
@@ -183,6 +185,29 @@ def test_stochastic_rounding_is_unbiased(devmath, half):
         x = float(np.float32(f)) + float(np.float32(d))
         ulp_lo = float(np.spacing(dt(min(abs(x), f) * 0.999)))
         assert abs(out.mean() - x) < 0.25 * ulp_lo, (f, d, (out.mean() - x) / ulp_lo)
+
+
+def test_pair_rounding_is_unbiased_and_uncorrelated(devmath):
+    """Round<float>::apply_pair draws the noise of two populations from one
+    step of the sequence: each output takes one of the two neighbours of
+    f + d with mean f + d, and the two rounding errors of a cell are nearly
+    uncorrelated over the cells."""
+    n = 200000
+    out = np.zeros(2 * n)
+    dp = C.POINTER(C.c_double)
+    for f, d in ((0.0123456, 3.1e-7), (-0.0071, 2.2e-6), (0.3, -1.3e-8)):
+        devmath.dev_round_pair(f, d, n, 4321, out.ctypes.data_as(dp))
+        x = float(np.float32(f)) + float(np.float32(d))
+        lo = float(np.float32(x))
+        if lo > x:
+            lo = float(np.nextafter(np.float32(x), np.float32(-np.inf)))
+        hi = float(np.nextafter(np.float32(lo), np.float32(np.inf)))
+        ulp = hi - lo
+        a, b = out[0::2], out[1::2]
+        for v in (a, b):
+            assert set(np.unique(v)) <= {lo, hi}
+            assert abs(v.mean() - x) < 0.01 * ulp, (f, d, (v.mean() - x) / ulp)
+        assert abs(np.corrcoef(a, b)[0, 1]) < 0.02, np.corrcoef(a, b)[0, 1]
 
 
 def test_factored_d3q19_moments_match_the_table(devmath):
