@@ -167,22 +167,20 @@ __device__ __forceinline__ void pull_all(C* lam, const A* __restrict__ lin, int 
 
 // Per-cell bodies, shared by the single-lattice kernels and the batched ones.
 
-// Forward step of cell (x,y,z); returns its objective contribution F(f_t).
+// Forward step of cell (x,y,z) = index c from its loaded state f~_t (in f,
+// overwritten) and design value g; returns its objective contribution F(f_t).
 template <int LAT, int COLL, class S>
-__device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, int x, int y, int z) {
+__device__ __forceinline__ typename Store<S>::C forward_cell_from(const KParams& p, int x, int y,
+                                                                  int z, int c,
+                                                                  typename Store<S>::C* f,
+                                                                  typename Store<S>::C g) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
-  using G = typename GammaT<S>::T;
   constexpr bool SHIFT = Store<S>::SHIFT;
   C objv = C(0.);
-  if (x < p.nx && y < p.ny) {
-    const int c = (z * p.ny + y) * p.nx + x;
-    const S* __restrict__ fin = (const S*)p.fin;
+  {
     S* __restrict__ fout = (S*)p.fout;
-    C f[L::Q];
-    load_state<LAT, S>(f, fin, c, (int)p.P);
     if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
-    const C g = C(((const G*)p.gamma)[c]);
     if (p.eval_obj) objv = objective_cell<LAT, SHIFT>(f, g, x, y, z, p);
     const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C rho, jx, jy, jz;
@@ -214,6 +212,22 @@ __device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, i
       }
       push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
     }
+  }
+  return objv;
+}
+
+// Forward step of cell (x,y,z); returns its objective contribution F(f_t).
+template <int LAT, int COLL, class S>
+__device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, int x, int y, int z) {
+  using L = Lattice<LAT>;
+  using C = typename Store<S>::C;
+  using G = typename GammaT<S>::T;
+  C objv = C(0.);
+  if (x < p.nx && y < p.ny) {
+    const int c = (z * p.ny + y) * p.nx + x;
+    C f[L::Q];
+    load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
+    objv = forward_cell_from<LAT, COLL, S>(p, x, y, z, c, f, C(((const G*)p.gamma)[c]));
   }
   return objv;
 }

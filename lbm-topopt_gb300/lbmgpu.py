@@ -41,8 +41,10 @@ OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX, OBJ_OUTFLOW = 0, 1,
 SCHEDULE_DYNAMIC, SCHEDULE_STATIC = 0, 1
 MAX_BC = 8
 
-STATUS_TEXT = {0: "ok", -1: "bad argument", -2: "unsupported", -3: "CUDA error",
-               -4: "out of memory", -5: "call out of order", -6: "non-finite value"}
+ERR_ARG, ERR_SUP, ERR_CUDA, ERR_MEM, ERR_STATE, ERR_NONFINITE = -1, -2, -3, -4, -5, -6
+STATUS_TEXT = {0: "ok", ERR_ARG: "bad argument", ERR_SUP: "unsupported", ERR_CUDA: "CUDA error",
+               ERR_MEM: "out of memory", ERR_STATE: "call out of order",
+               ERR_NONFINITE: "non-finite value"}
 
 # MRT rates: d'Humieres defaults (dynamics/MRT3d.hh:9-22) and the 2D ones
 # (dynamics/incompressibleMRT2d.hh:88-90)
