@@ -260,24 +260,36 @@ __host__ __device__ inline bool in_box(const int* b, int x, int y, int z) {
 // ---------------------------------------------------------------------------
 // Interpolations (core/interpolationFunctions.hh:17-54).
 
-// a / b; FP32 on the GPU takes the fast division (about 2 units in the last
-// place for the denominators here, q + s in [q, q + 1]), FP64 stays exact.
-template <class C>
-__device__ __forceinline__ C interp_div(C a, C b) {
+// a / b for the FP32 interpolations: the fast division on the GPU (about 2
+// units in the last place for the denominators here, q + s in [q, q + 1]).
+__device__ __forceinline__ float interp_div(float a, float b) {
 #if defined(__CUDA_ARCH__)
-  if constexpr (sizeof(C) == 4) return __fdividef(a, b);
-#endif
+  return __fdividef(a, b);
+#else
   return a / b;
+#endif
 }
 
+// BPInterpolation (core/interpolationFunctions.hh:18-25).  FP64 evaluates the
+// reference's expressions; FP32 the algebraically equal q(1-s)/(q+s) and
+// -q(1+q)/(q+s)^2 with the fast division, which are exactly 0 in fluid cells
+// (s = 1) whatever the division's rounding: 1 - s(1+q)/(q+s) is 0 there only
+// if the quotient rounds to exactly 1.
 template <class C>
 __device__ __forceinline__ C bp(C s, C q) {
-  return C(1.) - interp_div(s * (C(1.) + q), q + s);
+  if constexpr (sizeof(C) == 4)
+    return interp_div(q * (C(1.) - s), q + s);
+  else
+    return C(1.) - s * (C(1.) + q) / (q + s);
 }
 template <class C>
 __device__ __forceinline__ C bp_diff(C s, C q) {
-  const C r = interp_div(C(1.), q + s);
-  return (C(1.) + q) * r * (s * r - C(1.));
+  if constexpr (sizeof(C) == 4) {
+    const C r = interp_div(C(1.), q + s);
+    return -(q * (C(1.) + q)) * (r * r);
+  } else {
+    return (-(C(1.) + q) / (q + s) + s * (C(1.) + q) / ((q + s) * (q + s)));
+  }
 }
 template <class C>
 __device__ __forceinline__ C ramp(C s, C q, C ck) {

@@ -256,6 +256,17 @@ void dev_mrt3d_back(const double* r, double* out) {
     out[d + 9] = mrt3d_odd_back<d>(r);
   });
 }
+// The porosity interpolation BP_q(s) and its derivative in FP32 (fp32 != 0)
+// or FP64: out[0] = BP, out[1] = BP'.
+void dev_bp(int fp32, double s, double q, double* out) {
+  if (fp32) {
+    out[0] = (double)bp<float>((float)s, (float)q);
+    out[1] = (double)bp_diff<float>((float)s, (float)q);
+  } else {
+    out[0] = bp<double>(s, q);
+    out[1] = bp_diff<double>(s, q);
+  }
+}
 // Transposed even rows for moment adjoints m: G_0, then G_d for d = 1..9.
 void dev_mrt3d_rows_t(const double* m, double* out) {
   const Mrt3dEvenRowsT<double> gt(m);

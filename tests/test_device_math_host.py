@@ -48,6 +48,8 @@ def devmath():
     lib.dev_reverse_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
     lib.dev_round.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round.restype = None
+    lib.dev_bp.argtypes = [C.c_int, C.c_double, C.c_double, dp]
+    lib.dev_bp.restype = None
     lib.dev_round_pair.argtypes = [C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round_pair.restype = None
     ip = C.POINTER(C.c_int)
@@ -185,6 +187,31 @@ def test_stochastic_rounding_is_unbiased(devmath, half):
         x = float(np.float32(f)) + float(np.float32(d))
         ulp_lo = float(np.spacing(dt(min(abs(x), f) * 0.999)))
         assert abs(out.mean() - x) < 0.25 * ulp_lo, (f, d, (out.mean() - x) / ulp_lo)
+
+
+def test_porosity_interpolation(devmath):
+    """BP_q(s) = 1 - s(1+q)/(q+s) (interpolationFunctions.hh:18-25): the FP32
+    form q(1-s)/(q+s) is exactly 0 in fluid cells (s = 1) and 1 in solid
+    ones, matches the FP64 value to FP32 rounding, and both derivatives match
+    central differences of FP64."""
+    dp = C.POINTER(C.c_double)
+    out = np.zeros(2)
+    for q in (0.1, 0.01, 1.0):
+        devmath.dev_bp(1, 1.0, q, out.ctypes.data_as(dp))
+        assert out[0] == 0.0
+        devmath.dev_bp(1, 0.0, q, out.ctypes.data_as(dp))
+        assert abs(out[0] - 1.0) < 1e-6
+        for s in np.linspace(0, 1, 11):
+            ref = np.zeros(2)
+            devmath.dev_bp(0, s, q, ref.ctypes.data_as(dp))
+            assert abs(ref[0] - (1 - s * (1 + q) / (q + s))) < 1e-15
+            devmath.dev_bp(1, s, q, out.ctypes.data_as(dp))
+            assert abs(out[0] - ref[0]) < 1e-6
+            assert abs(out[1] - ref[1]) < 1e-6 * abs(ref[1])
+            hi, lo = np.zeros(2), np.zeros(2)
+            devmath.dev_bp(0, s + 1e-6, q, hi.ctypes.data_as(dp))
+            devmath.dev_bp(0, s - 1e-6, q, lo.ctypes.data_as(dp))
+            assert abs((hi[0] - lo[0]) / 2e-6 - ref[1]) < 1e-6 * abs(ref[1])
 
 
 def test_pair_rounding_is_unbiased_and_uncorrelated(devmath):
