@@ -239,7 +239,6 @@ struct KParams {
   const void* lam_in;      // eta_{t+1}
   void* lam_out;           // eta_t
   double* sens;
-  int* error_flag;         // set to a non-zero code on a non-finite result
 };
 
 template <class C>
