@@ -386,7 +386,7 @@ int ensure_stage(lbm_handle* h) {
 }
 
 // Objective summed over time steps without a per-step reduction: zero the
-// block partials, let every step's reduction add into them, sum them once.
+// warp partials, let every step's reduction add into them, sum them once.
 int begin_accumulate(lbm_handle* h, cudaStream_t st) {
   CUDA_OR_FAIL(h, cudaMemsetAsync(h->partial, 0, h->partial_cap * sizeof(double), st));
   h->accumulate = true;
@@ -555,10 +555,11 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   h->geo = make_geometry(c.nx, c.ny, h->cfg.nz, bx, by);
   h->geo_fwd = h->geo;
   h->geo_adj = h->geo;
-  // partial sums: room for the largest grid any tuned shape can give
+  // partial sums: one slot per warp of the largest grid any tuned shape gives
   for (const auto& sh : kShapes) {
     Geometry g = make_geometry(c.nx, c.ny, h->cfg.nz, sh[0], sh[1]);
-    if (g.nblocks > h->partial_cap) h->partial_cap = g.nblocks;
+    const size_t slots = (size_t)g.nblocks * (size_t)(sh[0] * sh[1] / 32);
+    if (slots > h->partial_cap) h->partial_cap = slots;
   }
 
 #define ALLOC(ptr, bytes)                                                                  \
@@ -1098,7 +1099,8 @@ int lbm_set_launch_shape(lbm_handle* h, int which, int bx, int by) {
   if (bx < 32 || bx % 32 != 0 || by < 1 || (bx * by != 128 && bx * by != 256))
     return fail(h, LBM_ERR_ARG, "block %dx%d: bx must be a multiple of 32 and bx*by 128 or 256", bx, by);
   Geometry g = make_geometry(h->cfg.nx, h->cfg.ny, h->cfg.nz, bx, by);
-  if (g.nblocks > h->partial_cap) return fail(h, LBM_ERR_ARG, "block %dx%d gives too many blocks", bx, by);
+  if ((size_t)g.nblocks * (size_t)(bx * by / 32) > h->partial_cap)
+    return fail(h, LBM_ERR_ARG, "block %dx%d gives too many blocks", bx, by);
   (which == 0 ? h->geo_fwd : h->geo_adj) = g;
   return LBM_OK;
 }

@@ -1823,17 +1823,16 @@ __device__ __forceinline__ void grid_reduce_v(C v, const KParams& p, unsigned bi
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nthr = blockDim.x * blockDim.y;
   if (p.accumulate) {
-    // Sum over time steps: every block adds its own sum to its own slot, so
-    // no counter, fence or atomic is needed; blocks whose cells contribute
-    // nothing (e.g. away from the pressure-drop strips) stop here.
-    if (!__syncthreads_or(v != C(0.))) return;
-    v = warp_sum(v);
-    if ((tid & 31) == 0) sh[tid >> 5] = (double)v;
-    __syncthreads();
-    if (tid == 0) {
-      double s = 0.;
-      for (int w = 0; w < (nthr + 31) / 32; ++w) s += sh[w];
-      p.partial[bid] += s;
+    // Sum over time steps: every warp adds its own sum to its own slot
+    // (block * warps per block + warp) once per launch, so neither a counter,
+    // a fence nor a barrier is needed and the additions come in a fixed
+    // order; warps whose cells contribute nothing (e.g. away from the
+    // pressure-drop strips) skip the shuffle tree.  The add's result is
+    // unused, so the warp does not wait for the slot's old value.
+    if (__any_sync(0xffffffffu, v != C(0.))) {
+      v = warp_sum(v);
+      if ((tid & 31) == 0)
+        atomicAdd(&p.partial[(size_t)bid * (size_t)(nthr >> 5) + (size_t)(tid >> 5)], (double)v);
     }
     return;
   }

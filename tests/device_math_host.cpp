@@ -21,6 +21,7 @@ inline void __syncthreads() {}
 inline int __syncthreads_or(int v) { return v; }
 inline void __threadfence() {}
 inline unsigned atomicAdd(unsigned* p, unsigned v) { unsigned o = *p; *p += v; return o; }
+inline double atomicAdd(double* p, double v) { double o = *p; *p += v; return o; }
 inline float __ldcs(const float* p) { return *p; }
 inline void __stcs(float* p, float v) { *p = v; }
 inline float __uint_as_float(unsigned u) { float f; memcpy(&f, &u, 4); return f; }
