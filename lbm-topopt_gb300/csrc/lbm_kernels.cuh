@@ -330,8 +330,19 @@ __device__ __forceinline__ typename Store<S>::C objective_only_cell(const KParam
   return v;
 }
 
+// Start of every time-step kernel.  The step kernels are launched with
+// programmatic stream serialisation (launch_overlapped): their CTAs may be
+// scheduled while the previous kernel in the stream drains its last wave.
+// Each CTA lets the next launch proceed, then waits until the previous grid
+// has completed and its writes are visible, before it touches memory.
+__device__ __forceinline__ void step_prologue() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd) k_forward(KParams p) {
+  step_prologue();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const auto objv = forward_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
@@ -340,6 +351,7 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd) k_forward(K
 
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj) k_adjoint(KParams p) {
+  step_prologue();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   adjoint_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
@@ -363,6 +375,7 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     k_forward_batch(const __grid_constant__ BatchParams bp) {
+  step_prologue();
   for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
     int i = 0;
     while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
@@ -379,6 +392,7 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj)
     k_adjoint_batch(const __grid_constant__ BatchParams bp) {
+  step_prologue();
   for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
     int i = 0;
     while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
@@ -530,15 +544,32 @@ __global__ void k_gamma(const double* __restrict__ src, G* __restrict__ dst, lon
 
 // ---------------------------------------------------------------------------
 
+// Launch of a kernel that begins with step_prologue, with programmatic stream
+// serialisation allowed.
+template <class K, class P>
+void launch_overlapped(K kern, dim3 grid, dim3 block, cudaStream_t st, const P& arg) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, arg);
+}
+
 template <int LAT, int COLL, class S>
 struct OpsImpl {
   static void launch_batch(int kind, dim3 grid, dim3 block, cudaStream_t st, const BatchParams& bp) {
     switch (kind) {
       case K_FORWARD:
-        k_forward_batch<LAT, COLL, S><<<grid, block, 0, st>>>(bp);
+        launch_overlapped(k_forward_batch<LAT, COLL, S>, grid, block, st, bp);
         break;
       case K_ADJOINT:
-        k_adjoint_batch<LAT, COLL, S><<<grid, block, 0, st>>>(bp);
+        launch_overlapped(k_adjoint_batch<LAT, COLL, S>, grid, block, st, bp);
         break;
       case K_OBJECTIVE:
         k_objective_batch<LAT, S><<<grid, block, 0, st>>>(bp);
@@ -563,10 +594,10 @@ struct OpsImpl {
                      double* aux) {
     switch (kind) {
       case K_FORWARD:
-        k_forward<LAT, COLL, S><<<grid, block, 0, st>>>(p);
+        launch_overlapped(k_forward<LAT, COLL, S>, grid, block, st, p);
         break;
       case K_ADJOINT:
-        k_adjoint<LAT, COLL, S><<<grid, block, 0, st>>>(p);
+        launch_overlapped(k_adjoint<LAT, COLL, S>, grid, block, st, p);
         break;
       case K_OBJECTIVE:
         k_objective<LAT, S><<<grid, block, 0, st>>>(p);
