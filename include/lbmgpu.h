@@ -308,9 +308,13 @@ const char* lbm_batch_last_error(const lbm_batch* b);
 /* The handle of lattice i (owned by the batch): set its design, read its state
  * and sensitivities with the single-lattice entry points. */
 int lbm_batch_handle(lbm_batch* b, int i, lbm_handle** h);
-/* Pick the block shape of the batched step kernels (states are re-initialised). */
+/* Pick the block shapes of the batched forward and reverse step kernels,
+ * each timed on its own (states are re-initialised). */
 int lbm_batch_autotune(lbm_batch* b, int nsteps);
+/* Block shape of the batched forward (and objective) kernels. */
 int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by);
+/* Block shape of the batched reverse step kernel. */
+int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by);
 /* nsteps forward steps of every lattice from its current state; J[i] (may be
  * NULL) gets lattice i's objective sum as lbm_forward would. */
 int lbm_batch_forward(lbm_batch* b, int nsteps, double* J);

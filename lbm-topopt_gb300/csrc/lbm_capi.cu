@@ -1205,7 +1205,8 @@ struct lbm_batch {
   lbm_handle* h[LBM_MAX_BATCH] = {};
   BatchOps ops;
   cudaStream_t stream = nullptr;
-  int bx = 128, by = 2;
+  int bx = 128, by = 2;     // block shape of the forward and objective kernels
+  int abx = 128, aby = 2;   // block shape of the reverse step kernel
   int nsm = 1;
   int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
   cudaGraphExec_t graph = nullptr;
@@ -1240,30 +1241,47 @@ int bfail(lbm_batch* b, int code, const char* fmt, ...) {
   } while (0)
 
 // Persistent grid: resident blocks of kernel `kind` times SMs, at most the work.
+// Block shape of a batched kernel: the reverse step has its own.
+dim3 batch_block(const lbm_batch* b, int kind) {
+  return kind == K_ADJOINT ? dim3(b->abx, b->aby) : dim3(b->bx, b->by);
+}
+
 int batch_grid(lbm_batch* b, int kind, int total) {
   int per_sm = 1;
   const void* k = b->ops.kernel(kind);
-  if (k) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, b->bx * b->by, 0);
+  const dim3 blk = batch_block(b, kind);
+  if (k) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, blk.x * blk.y, 0);
   if (per_sm < 1) per_sm = 1;
   int g = per_sm * b->nsm;
   return g < total ? g : total;
 }
 
-void batch_layout(lbm_batch* b, BatchParams& bp) {
+void batch_layout(lbm_batch* b, BatchParams& bp, int kind) {
+  const dim3 blk = batch_block(b, kind);
   bp.n = b->n;
   int start = 0;
   for (int i = 0; i < b->n; ++i) {
     const lbm_handle* h = b->h[i];
-    bp.gx[i] = (h->cfg.nx + b->bx - 1) / b->bx;
-    bp.gy[i] = (h->cfg.ny + b->by - 1) / b->by;
+    bp.gx[i] = (h->cfg.nx + (int)blk.x - 1) / (int)blk.x;
+    bp.gy[i] = (h->cfg.ny + (int)blk.y - 1) / (int)blk.y;
     bp.start[i] = start;
     start += bp.gx[i] * bp.gy[i] * h->cfg.nz;
   }
   bp.start[b->n] = start;
 }
 
+// Persistent grids of the batched kernels for the current block shapes.
+void batch_set_grids(lbm_batch* b) {
+  BatchParams bp;
+  batch_layout(b, bp, K_FORWARD);
+  b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
+  b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
+  batch_layout(b, bp, K_ADJOINT);
+  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
+}
+
 int batch_launch(lbm_batch* b, int kind, const BatchParams& bp, int grid) {
-  b->ops.launch(kind, dim3(grid), dim3(b->bx, b->by), b->stream, bp);
+  b->ops.launch(kind, dim3(grid), batch_block(b, kind), b->stream, bp);
   b->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, "batched launch %d: %s", kind, cudaGetErrorString(e));
@@ -1282,7 +1300,7 @@ void* batch_buffer(lbm_handle* h, int b) {
 // results[i] (may be null) gets F of lattice i.
 int batch_forward_bufs(lbm_batch* b, int in, int out, double* const* results) {
   BatchParams bp;
-  batch_layout(b, bp);
+  batch_layout(b, bp, K_FORWARD);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
@@ -1308,7 +1326,7 @@ int batch_forward(lbm_batch* b, double* const* results) {
 
 int batch_objective(lbm_batch* b, int buf, double* const* results) {
   BatchParams bp;
-  batch_layout(b, bp);
+  batch_layout(b, bp, K_OBJECTIVE);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
@@ -1322,7 +1340,7 @@ int batch_objective(lbm_batch* b, int buf, double* const* results) {
 
 int batch_adjoint(lbm_batch* b, int buf) {
   BatchParams bp;
-  batch_layout(b, bp);
+  batch_layout(b, bp, K_ADJOINT);
   for (int i = 0; i < b->n; ++i) {
     lbm_handle* h = b->h[i];
     KParams& p = bp.p[i];
@@ -1504,14 +1522,10 @@ int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out) {
   }
   cudaEventCreate(&b->ev[0]);
   cudaEventCreate(&b->ev[1]);
-  // default shape: 128x2, one of the autotuner's shapes (partial sums are sized for all)
-  b->bx = 128;
-  b->by = 2;
-  BatchParams bp;
-  batch_layout(b, bp);
-  b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
-  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
-  b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
+  // default shapes: 128x2, one of the autotuner's shapes (partial sums are sized for all)
+  b->bx = b->abx = 128;
+  b->by = b->aby = 2;
+  batch_set_grids(b);
   b->grid_copy = 4 * b->nsm;
   *out = b;
   return LBM_OK;
@@ -1551,39 +1565,49 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
     h->have_adjoint = true;
     h->t = 1;
   }
-  float best = 1e30f;
-  int bbx = b->bx, bby = b->by;
-  for (const auto& sh : kShapes) {
-    b->bx = sh[0];
-    b->by = sh[1];
-    BatchParams bp;
-    batch_layout(b, bp);
-    b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
-    b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
-    if ((rc = batch_forward(b, nullptr)) || (rc = batch_adjoint(b, kCurState))) return rc;
-    cudaEventRecord(b->ev[0], b->stream);
-    for (int k = 0; k < nsteps && !rc; ++k) {
-      rc = batch_forward(b, nullptr);
-      if (!rc) rc = batch_adjoint(b, kCurState);
+  // each kernel on its own: every shape for the forward step, then every
+  // shape for the reverse step
+  float best_f = 1e30f, best_a = 1e30f;
+  int fbx = b->bx, fby = b->by, abx = b->abx, aby = b->aby;
+  for (int which = 0; which < 2; ++which) {
+    for (const auto& sh : kShapes) {
+      if (which == 0) {
+        b->bx = sh[0];
+        b->by = sh[1];
+      } else {
+        b->abx = sh[0];
+        b->aby = sh[1];
+      }
+      batch_set_grids(b);
+      rc = which == 0 ? batch_forward(b, nullptr) : batch_adjoint(b, kCurState);
+      if (rc) return rc;
+      cudaEventRecord(b->ev[0], b->stream);
+      for (int k = 0; k < nsteps && !rc; ++k)
+        rc = which == 0 ? batch_forward(b, nullptr) : batch_adjoint(b, kCurState);
+      cudaEventRecord(b->ev[1], b->stream);
+      if (rc) return rc;
+      BCUDA(b, cudaStreamSynchronize(b->stream));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+      if (which == 0 && ms < best_f) {
+        best_f = ms;
+        fbx = sh[0];
+        fby = sh[1];
+      }
+      if (which == 1 && ms < best_a) {
+        best_a = ms;
+        abx = sh[0];
+        aby = sh[1];
+      }
     }
-    cudaEventRecord(b->ev[1], b->stream);
-    if (rc) return rc;
-    BCUDA(b, cudaStreamSynchronize(b->stream));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
-    if (ms < best) {
-      best = ms;
-      bbx = sh[0];
-      bby = sh[1];
+    if (which == 0) {
+      b->bx = fbx;
+      b->by = fby;
     }
   }
-  b->bx = bbx;
-  b->by = bby;
-  BatchParams bp;
-  batch_layout(b, bp);
-  b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
-  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
-  b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
+  b->abx = abx;
+  b->aby = aby;
+  batch_set_grids(b);
   if ((rc = batch_init(b, kCurState))) return rc;
   BCUDA(b, cudaStreamSynchronize(b->stream));
   return LBM_OK;
@@ -1593,6 +1617,13 @@ int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by) {
   if (!b || !bx || !by) return bfail(nullptr, LBM_ERR_ARG, "null argument");
   *bx = b->bx;
   *by = b->by;
+  return LBM_OK;
+}
+
+int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by) {
+  if (!b || !bx || !by) return bfail(nullptr, LBM_ERR_ARG, "null argument");
+  *bx = b->abx;
+  *by = b->aby;
   return LBM_OK;
 }
 

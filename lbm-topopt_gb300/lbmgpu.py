@@ -203,6 +203,7 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_batch_handle": (C.c_int, [H, C.c_int, C.POINTER(H)]),
         "lbm_batch_autotune": (C.c_int, [H, C.c_int]),
         "lbm_batch_get_launch_shape": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_batch_get_reverse_shape": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_batch_forward": (C.c_int, [H, C.c_int, dp]),
         "lbm_batch_gradient": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp, C.POINTER(dp),
                                          C.POINTER(CGradStats)]),
@@ -520,9 +521,16 @@ class Batch:
         return len(self.views)
 
     def autotune(self, nsteps: int = 3):
+        """Tune the block shapes; returns the forward one (reverse_shape()
+        gives the other)."""
         self._check(self.lib.lbm_batch_autotune(self.b, int(nsteps)))
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_batch_get_launch_shape(self.b, C.byref(bx), C.byref(by)))
+        return bx.value, by.value
+
+    def reverse_shape(self):
+        bx, by = C.c_int(), C.c_int()
+        self._check(self.lib.lbm_batch_get_reverse_shape(self.b, C.byref(bx), C.byref(by)))
         return bx.value, by.value
 
     def forward(self, nsteps: int):
