@@ -281,10 +281,21 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
         lout[q * (int)p.P + c] = A(lam[q]);
       });
     } else {
+      // flow pairs (k, k + HALF) share one draw and packed arithmetic; the
+      // rest population and the temperature lattice round one by one
       Dither rnd((unsigned)c, p.key_adj);
-      static_for<L::Q>([&](auto Q_) {
-        constexpr int q = decltype(Q_)::value;
-        lout[q * (int)p.P + c] = Round<A>::apply(lam[q], d[q], rnd);
+      const int P = (int)p.P;
+      lout[c] = Round<A>::apply(lam[0], d[0], rnd);
+      static_for<L::HALF>([&](auto D_) {
+        constexpr int k = decltype(D_)::value + 1, o = k + L::HALF;
+        A a, b;
+        Round<A>::apply_pair(lam[k], lam[o], d[k], d[o], rnd, a, b);
+        lout[k * P + c] = a;
+        lout[o * P + c] = b;
+      });
+      static_for<L::Q - L::QF>([&](auto T_) {
+        constexpr int q = decltype(T_)::value + L::QF;
+        lout[q * P + c] = Round<A>::apply(lam[q], d[q], rnd);
       });
     }
     p.sens[c] += (double)dg;
