@@ -261,8 +261,9 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnapshots, int schedul
 int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms);
 
 /* Time every candidate thread-block shape of the forward and reverse step
- * kernels for nsteps steps each on this handle's lattice and keep the
- * fastest (the tile-shape autotuner).  Needs a design and a state; the state
+ * kernels (and both register variants of the reverse step) for nsteps steps
+ * each on this handle's lattice and keep the fastest (the tile-shape
+ * autotuner).  Needs a design and a state; the state
  * is left unchanged and the adjoint and sensitivity fields are zeroed. */
 int lbm_autotune(lbm_handle* h, int nsteps);
 
@@ -274,6 +275,19 @@ int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by);
  * bx * by in {128, 256}.  No reference counterpart (the reference has no
  * launch geometry). */
 int lbm_set_launch_shape(lbm_handle* h, int which, int bx, int by);
+
+/* Reverse step kernel variant: 0 the default register budget, 1 one more
+ * resident thread block per SM with fewer registers per thread (faster where
+ * the extra warps hide more memory latency than the spills cost; lbm_autotune
+ * times both).  Results agree to FP32 rounding: under the tighter register
+ * budget the compiler may fuse a few multiply-adds differently (measured
+ * 9e-10 of max |dJ/dgamma| on a D2Q9 channel; bit-identical on D3Q19 MRT and
+ * the thermal model).  Set the variant explicitly for bitwise reproducible
+ * FP32 gradients across tuning runs.  FP64 storage has only variant 0 (1
+ * returns LBM_ERR_SUP).  No reference counterpart. */
+int lbm_set_reverse_variant(lbm_handle* h, int lean);
+/* The reverse step variant in use (0 or 1), negative on error. */
+int lbm_get_reverse_variant(const lbm_handle* h);
 
 /* Select the CUDA device (ordinal) that handles created afterwards by this
  * thread use (one process per GPU: the rank's local GPU). */
@@ -309,12 +323,16 @@ const char* lbm_batch_last_error(const lbm_batch* b);
  * and sensitivities with the single-lattice entry points. */
 int lbm_batch_handle(lbm_batch* b, int i, lbm_handle** h);
 /* Pick the block shapes of the batched forward and reverse step kernels,
- * each timed on its own (states are re-initialised). */
+ * each timed on its own, and the reverse step's register variant (states are
+ * re-initialised). */
 int lbm_batch_autotune(lbm_batch* b, int nsteps);
 /* Block shape of the batched forward (and objective) kernels. */
 int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by);
 /* Block shape of the batched reverse step kernel. */
 int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by);
+/* Register variant of the batched reverse step (as lbm_set_reverse_variant). */
+int lbm_batch_set_reverse_variant(lbm_batch* b, int lean);
+int lbm_batch_get_reverse_variant(const lbm_batch* b);
 /* nsteps forward steps of every lattice from its current state; J[i] (may be
  * NULL) gets lattice i's objective sum as lbm_forward would. */
 int lbm_batch_forward(lbm_batch* b, int nsteps, double* J);

@@ -60,6 +60,7 @@ struct lbm_handle {
   Geometry geo;       // initialisation / export kernels
   Geometry geo_fwd;   // forward step (autotuned)
   Geometry geo_adj;   // reverse step (autotuned)
+  bool adj_lean = false;   // reverse step: the register-lean variant (autotuned)
   bool tuned = false;
   size_t partial_cap = 0;
   void* f[2] = {nullptr, nullptr};
@@ -361,7 +362,9 @@ KParams base_params(const lbm_handle* h, int t) {
 }
 
 int launch(lbm_handle* h, int kind, const KParams& p, double* aux) {
-  const Geometry& g = kind == K_FORWARD ? h->geo_fwd : kind == K_ADJOINT ? h->geo_adj : h->geo;
+  const Geometry& g = kind == K_FORWARD                              ? h->geo_fwd
+                      : (kind == K_ADJOINT || kind == K_ADJOINT_LEAN) ? h->geo_adj
+                                                                       : h->geo;
   h->launch(kind, g.grid, g.block, h->stream, p, aux);
   h->launches++;
   cudaError_t e = cudaGetLastError();
@@ -444,7 +447,7 @@ int adjoint_at(lbm_handle* h, const void* f) {
   p.lam_in = h->lam[h->lcur];
   p.lam_out = h->lam[1 - h->lcur];
   p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
-  int rc = launch(h, K_ADJOINT, p, nullptr);
+  int rc = launch(h, h->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, p, nullptr);
   if (rc) return rc;
   h->lcur ^= 1;
   return 0;
@@ -1062,12 +1065,16 @@ int lbm_autotune(lbm_handle* h, int nsteps) {
   if (h->t < 1) h->t = 1;
   float best_f = 1e30f, best_a = 1e30f;
   Geometry bf = h->geo_fwd, ba = h->geo_adj;
+  bool blean = h->adj_lean;
   const int nx = h->cfg.nx;
+  const int nlean = h->cfg.storage == LBM_STORE_FP64 ? 1 : 2;   // FP64 has no lean variant
   for (const auto& sh : kShapes) {
     if (sh[0] > ((nx + 31) / 32) * 32 && sh[0] > 32) continue;
     Geometry g = make_geometry(nx, h->cfg.ny, h->cfg.nz, sh[0], sh[1]);
-    for (int which = 0; which < 2; ++which) {
+    for (int which = 0; which < 1 + nlean; ++which) {
+      // which: 0 forward, 1 reverse, 2 reverse (lean variant)
       (which == 0 ? h->geo_fwd : h->geo_adj) = g;
+      if (which >= 1) h->adj_lean = which == 2;
       // one untimed launch, then nsteps timed
       rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
       if (rc) { cudaFree(keep); return rc; }
@@ -1078,11 +1085,12 @@ int lbm_autotune(lbm_handle* h, int nsteps) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
       if (which == 0 && ms < best_f) { best_f = ms; bf = g; }
-      if (which == 1 && ms < best_a) { best_a = ms; ba = g; }
+      if (which >= 1 && ms < best_a) { best_a = ms; ba = g; blean = which == 2; }
     }
   }
   h->geo_fwd = bf;
   h->geo_adj = ba;
+  h->adj_lean = blean;
   h->tuned = true;
   h->cur = cur_keep;
   h->t = t_keep;
@@ -1111,6 +1119,20 @@ int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by) {
   *bx = g.block.x;
   *by = g.block.y;
   return LBM_OK;
+}
+
+int lbm_set_reverse_variant(lbm_handle* h, int lean) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (lean != 0 && lean != 1) return fail(h, LBM_ERR_ARG, "variant %d is neither 0 nor 1", lean);
+  if (lean && h->cfg.storage == LBM_STORE_FP64)
+    return fail(h, LBM_ERR_SUP, "FP64 storage has no register-lean reverse variant");
+  h->adj_lean = lean == 1;
+  return LBM_OK;
+}
+
+int lbm_get_reverse_variant(const lbm_handle* h) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  return h->adj_lean ? 1 : 0;
 }
 
 int lbm_select_device(int ordinal) {
@@ -1207,6 +1229,7 @@ struct lbm_batch {
   cudaStream_t stream = nullptr;
   int bx = 128, by = 2;     // block shape of the forward and objective kernels
   int abx = 128, aby = 2;   // block shape of the reverse step kernel
+  bool adj_lean = false;    // reverse step: the register-lean variant
   int nsm = 1;
   int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
   cudaGraphExec_t graph = nullptr;
@@ -1243,7 +1266,7 @@ int bfail(lbm_batch* b, int code, const char* fmt, ...) {
 // Persistent grid: resident blocks of kernel `kind` times SMs, at most the work.
 // Block shape of a batched kernel: the reverse step has its own.
 dim3 batch_block(const lbm_batch* b, int kind) {
-  return kind == K_ADJOINT ? dim3(b->abx, b->aby) : dim3(b->bx, b->by);
+  return (kind == K_ADJOINT || kind == K_ADJOINT_LEAN) ? dim3(b->abx, b->aby) : dim3(b->bx, b->by);
 }
 
 int batch_grid(lbm_batch* b, int kind, int total) {
@@ -1277,7 +1300,7 @@ void batch_set_grids(lbm_batch* b) {
   b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
   b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
   batch_layout(b, bp, K_ADJOINT);
-  b->grid_adj = batch_grid(b, K_ADJOINT, bp.start[b->n]);
+  b->grid_adj = batch_grid(b, b->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, bp.start[b->n]);
 }
 
 int batch_launch(lbm_batch* b, int kind, const BatchParams& bp, int grid) {
@@ -1350,7 +1373,7 @@ int batch_adjoint(lbm_batch* b, int buf) {
     p.lam_out = h->lam[1 - h->lcur];
     p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
   }
-  int rc = batch_launch(b, K_ADJOINT, bp, b->grid_adj);
+  int rc = batch_launch(b, b->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, bp, b->grid_adj);
   if (rc) return rc;
   for (int i = 0; i < b->n; ++i) b->h[i]->lcur ^= 1;
   return 0;
@@ -1566,10 +1589,12 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
     h->t = 1;
   }
   // each kernel on its own: every shape for the forward step, then every
-  // shape for the reverse step
+  // shape and both register variants for the reverse step
   float best_f = 1e30f, best_a = 1e30f;
   int fbx = b->bx, fby = b->by, abx = b->abx, aby = b->aby;
-  for (int which = 0; which < 2; ++which) {
+  bool alean = b->adj_lean;
+  const int nlean = b->h[0]->cfg.storage == LBM_STORE_FP64 ? 1 : 2;
+  for (int which = 0; which < 1 + nlean; ++which) {
     for (const auto& sh : kShapes) {
       if (which == 0) {
         b->bx = sh[0];
@@ -1577,6 +1602,7 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
       } else {
         b->abx = sh[0];
         b->aby = sh[1];
+        b->adj_lean = which == 2;
       }
       batch_set_grids(b);
       rc = which == 0 ? batch_forward(b, nullptr) : batch_adjoint(b, kCurState);
@@ -1594,10 +1620,11 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
         fbx = sh[0];
         fby = sh[1];
       }
-      if (which == 1 && ms < best_a) {
+      if (which >= 1 && ms < best_a) {
         best_a = ms;
         abx = sh[0];
         aby = sh[1];
+        alean = which == 2;
       }
     }
     if (which == 0) {
@@ -1605,6 +1632,7 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
       b->by = fby;
     }
   }
+  b->adj_lean = alean;
   b->abx = abx;
   b->aby = aby;
   batch_set_grids(b);
@@ -1625,6 +1653,22 @@ int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by) {
   *bx = b->abx;
   *by = b->aby;
   return LBM_OK;
+}
+
+int lbm_batch_set_reverse_variant(lbm_batch* b, int lean) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  if (lean != 0 && lean != 1) return bfail(b, LBM_ERR_ARG, "variant %d is neither 0 nor 1", lean);
+  if (lean && b->h[0]->cfg.storage == LBM_STORE_FP64)
+    return bfail(b, LBM_ERR_SUP, "FP64 storage has no register-lean reverse variant");
+  batch_destroy_graph(b);
+  b->adj_lean = lean == 1;
+  batch_set_grids(b);
+  return LBM_OK;
+}
+
+int lbm_batch_get_reverse_variant(const lbm_batch* b) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  return b->adj_lean ? 1 : 0;
 }
 
 int lbm_batch_forward(lbm_batch* b, int nsteps, double* J) {

@@ -31,10 +31,16 @@ template <int LAT, int COLL, class S>
 struct Occupancy {
   static constexpr int fwd = 5;
   static constexpr int adj = (LAT == LAT_D3Q19 && COLL == LBM_BGK) ? 3 : 4;
+  // the register-lean reverse variant: one more resident block per SM (the
+  // tuner picks it where the extra warps beat the spills, e.g. the D2Q9 BGK
+  // adjoint on lattices larger than L2)
+  static constexpr int adj_lean = adj + 1;
+  static constexpr bool has_lean = true;
 };
 template <int LAT, int COLL>
 struct Occupancy<LAT, COLL, double> {
-  static constexpr int fwd = 1, adj = 1;
+  static constexpr int fwd = 1, adj = 1, adj_lean = 1;
+  static constexpr bool has_lean = false;
 };
 
 template <class S>
@@ -360,8 +366,9 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd) k_forward(K
   if (p.eval_obj) grid_reduce(objv, p);
 }
 
-template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj) k_adjoint(KParams p) {
+template <int LAT, int COLL, class S, bool LEAN = false>
+__global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
+                                            : Occupancy<LAT, COLL, S>::adj) k_adjoint(KParams p) {
   step_prologue();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -400,8 +407,9 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
   }
 }
 
-template <int LAT, int COLL, class S>
-__global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::adj)
+template <int LAT, int COLL, class S, bool LEAN = false>
+__global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
+                                            : Occupancy<LAT, COLL, S>::adj)
     k_adjoint_batch(const __grid_constant__ BatchParams bp) {
   step_prologue();
   for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
@@ -582,6 +590,10 @@ struct OpsImpl {
       case K_ADJOINT:
         launch_overlapped(k_adjoint_batch<LAT, COLL, S>, grid, block, st, bp);
         break;
+      case K_ADJOINT_LEAN:
+        launch_overlapped(k_adjoint_batch<LAT, COLL, S, Occupancy<LAT, COLL, S>::has_lean>, grid,
+                          block, st, bp);
+        break;
       case K_OBJECTIVE:
         k_objective_batch<LAT, S><<<grid, block, 0, st>>>(bp);
         break;
@@ -595,6 +607,8 @@ struct OpsImpl {
         return (const void*)k_forward_batch<LAT, COLL, S>;
       case K_ADJOINT:
         return (const void*)k_adjoint_batch<LAT, COLL, S>;
+      case K_ADJOINT_LEAN:
+        return (const void*)k_adjoint_batch<LAT, COLL, S, Occupancy<LAT, COLL, S>::has_lean>;
       case K_OBJECTIVE:
         return (const void*)k_objective_batch<LAT, S>;
       default:
@@ -609,6 +623,10 @@ struct OpsImpl {
         break;
       case K_ADJOINT:
         launch_overlapped(k_adjoint<LAT, COLL, S>, grid, block, st, p);
+        break;
+      case K_ADJOINT_LEAN:
+        launch_overlapped(k_adjoint<LAT, COLL, S, Occupancy<LAT, COLL, S>::has_lean>, grid, block,
+                          st, p);
         break;
       case K_OBJECTIVE:
         k_objective<LAT, S><<<grid, block, 0, st>>>(p);

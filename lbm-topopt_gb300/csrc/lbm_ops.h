@@ -20,6 +20,7 @@ enum {
   K_MACROS,
   K_EXPORT_ADJ,
   K_GAMMA,
+  K_ADJOINT_LEAN,   // the reverse step with one more resident block per SM
 };
 
 typedef void (*LaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st, const KParams& p,

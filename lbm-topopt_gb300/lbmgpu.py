@@ -212,6 +212,10 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_autotune": (C.c_int, [H, C.c_int]),
         "lbm_get_launch_shape": (C.c_int, [H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
+        "lbm_set_reverse_variant": (C.c_int, [H, C.c_int]),
+        "lbm_get_reverse_variant": (C.c_int, [H]),
+        "lbm_batch_set_reverse_variant": (C.c_int, [H, C.c_int]),
+        "lbm_batch_get_reverse_variant": (C.c_int, [H]),
         "lbm_forward_steady": (C.c_int, [H, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int),
                                          C.POINTER(C.c_double)]),
         "lbm_get_dims": (C.c_int, [H, C.POINTER(C.c_int)]),
@@ -456,6 +460,17 @@ class Handle:
     def set_launch_shape(self, which: int, bx: int, by: int):
         self._check(self.lib.lbm_set_launch_shape(self.h, int(which), int(bx), int(by)))
 
+    def set_reverse_variant(self, lean: int):
+        """0: default register budget of the reverse step, 1: the register-lean
+        variant (one more resident block per SM); same results."""
+        self._check(self.lib.lbm_set_reverse_variant(self.h, int(lean)))
+
+    @property
+    def reverse_variant(self) -> int:
+        r = self.lib.lbm_get_reverse_variant(self.h)
+        self._check(min(r, 0))
+        return r
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._check(self.lib.lbm_get_launch_count(self.h, C.byref(n)))
@@ -532,6 +547,15 @@ class Batch:
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_batch_get_reverse_shape(self.b, C.byref(bx), C.byref(by)))
         return bx.value, by.value
+
+    def set_reverse_variant(self, lean: int):
+        self._check(self.lib.lbm_batch_set_reverse_variant(self.b, int(lean)))
+
+    @property
+    def reverse_variant(self) -> int:
+        r = self.lib.lbm_batch_get_reverse_variant(self.b)
+        self._check(min(r, 0))
+        return r
 
     def forward(self, nsteps: int):
         J = np.zeros(len(self))

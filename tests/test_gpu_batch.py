@@ -83,3 +83,20 @@ def test_batch_d3q19_fp32_autotuned():
             Js, ss, _ = h.gradient(40, 5)
         assert abs(Jb - Js) <= 1e-5 * abs(Js)
         assert rel_inf(sb, ss) < 1e-4
+
+
+def test_batch_reverse_variant_does_not_change_results():
+    """As for a single lattice: the batched reverse step's two register
+    variants agree to FP32 rounding."""
+    insts = uneven_2d(storage=G.STORE_FP32, n=50)
+    out = []
+    for lean in (0, 1):
+        with G.Batch([c for c, _ in insts]) as b:
+            b.set_reverse_variant(lean)
+            assert b.reverse_variant == lean
+            for i, (_, g) in enumerate(insts):
+                b[i].set_design(g)
+            out.append(b.gradient(50, 6, use_graph=True))
+    assert np.allclose(out[0][0], out[1][0], rtol=1e-12, atol=0)
+    for a, c in zip(out[0][1], out[1][1]):
+        assert np.abs(a - c).max() <= 1e-7 * np.abs(a).max()
