@@ -21,17 +21,25 @@ STORAGE = {"fp64": G.STORE_FP64, "fp32": G.STORE_FP32, "fp16": G.STORE_FP16}
 
 
 def build_workload(which: int, storage: int, size=None):
+    kw = {}
+    if size:
+        kw = dict(nx=size[0], ny=size[1])
+        if which == 3:
+            if len(size) != 3:
+                raise ValueError("workload 3 takes --size nx ny nz")
+            kw["nz"] = size[2]
+        elif len(size) != 2:
+            raise ValueError("2D workloads take --size nx ny")
     if which == 1:
+        if size:
+            raise ValueError("workload 1 has a fixed size")
         cfg, g, n = W.workload_config1(storage)
     elif which == 2:
-        cfg, g, n = W.workload_config2(storage)
+        cfg, g, n = W.workload_config2(storage, **kw)
     elif which == 3:
-        kw = {}
-        if size:
-            kw = dict(nx=size[0], ny=size[1], nz=size[2])
         cfg, g, n = W.workload_config3(storage, **kw)
     elif which == 4:
-        cfg, g, n = W.workload_config4(storage)
+        cfg, g, n = W.workload_config4(storage, **kw)
     else:
         raise ValueError("workload must be 1-4")
     return cfg, g, n
@@ -41,7 +49,8 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--workload", type=int, default=3)
     ap.add_argument("--storage", choices=sorted(STORAGE), default="fp32")
-    ap.add_argument("--size", type=int, nargs=3, default=None, help="nx ny nz (workload 3)")
+    ap.add_argument("--size", type=int, nargs="+", default=None,
+                    help="nx ny nz (workload 3) or nx ny (workloads 2 and 4)")
     ap.add_argument("--fwd", type=int, default=10)
     ap.add_argument("--adj", type=int, default=10)
     ap.add_argument("--autotune", action="store_true", help="pick block shapes first")
