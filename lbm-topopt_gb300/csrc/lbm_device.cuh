@@ -1654,6 +1654,24 @@ __host__ __device__ constexpr int lat_e(int i, int a) {
   return a == 0 ? L::ex(i) : a == 1 ? L::ey(i) : L::ez(i);
 }
 
+// e_i^T P e_i for a symmetric 3x3 P, the zero terms left out (the rest in the
+// order a, b = 0..DIM-1)
+template <int LAT, int i, class C>
+__device__ __forceinline__ C e_quad(const C (&P)[3][3]) {
+  using L = Lattice<LAT>;
+  C v = C(0.);
+  static_for<L::DIM>([&](auto A) {
+    constexpr int a = decltype(A)::value;
+    static_for<L::DIM>([&](auto B) {
+      constexpr int b = decltype(B)::value;
+      constexpr int eab = lat_e<L>(i, a) * lat_e<L>(i, b);
+      if constexpr (eab == 1) v += P[a][b];
+      if constexpr (eab == -1) v -= P[a][b];
+    });
+  });
+  return v;
+}
+
 // P_ab = sum_i e_ia e_ib f_i over the flow lattice
 template <int LAT, class C>
 __device__ __forceinline__ void second_moment(const C* f, C (&P)[3][3]) {
@@ -1780,22 +1798,23 @@ __device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg,
       P[a][a] -= rho / C(3.);
       tr += P[a][a];
     }
+    // P j once; per population only the lattice vector's nonzero components
+    // (products with a zero component are not folded away in IEEE arithmetic)
+    C pj[3] = {C(0.), C(0.), C(0.)};
+#pragma unroll
+    for (int a = 0; a < L::DIM; ++a)
+#pragma unroll
+      for (int b = 0; b < L::DIM; ++b) pj[a] += P[a][b] * j[b];
     const C cv = mp<C>(p).cv_diss;
     const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     const C tc = mp<C>(p).obj_weight;
+    const C a4 = C(4.) * alpha, c2 = cv * C(2.), tr3 = tr / C(3.);
     static_for<L::QF>([&](auto I) {
       constexpr int i = decltype(I)::value;
-      constexpr int e[3] = {L::ex(i), L::ey(i), L::ez(i)};
-      C pe = C(0.), pej = C(0.);
-#pragma unroll
-      for (int a = 0; a < L::DIM; ++a)
-#pragma unroll
-        for (int b = 0; b < L::DIM; ++b) {
-          pe += P[a][b] * C(e[a] * e[b]);
-          pej += P[a][b] * C(e[a]) * j[b];
-        }
-      C ej = C(e[0]) * j[0] + C(e[1]) * j[1] + C(e[2]) * j[2];
-      lam[i] += tc * (C(4.) * alpha * ej + cv * C(2.) * (pe - tr / C(3.) - C(2.) * pej));
+      const C ej = e_dot<LAT, i>(j[0], j[1], j[2]);
+      const C pej = e_dot<LAT, i>(pj[0], pj[1], pj[2]);   // e . P j
+      const C pe = e_quad<LAT, i>(P);                     // e . P e
+      lam[i] += tc * (a4 * ej + c2 * ((pe - tr3) - C(2.) * pej));
     });
     C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     dg += tc * (C(2.) * (C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q))) * jj);
