@@ -339,6 +339,20 @@ __device__ __forceinline__ void flow_macros(const C* f, C& rho, C& jx, C& jy, C&
   }
 }
 
+// sum_a e_ia j_a with the zero terms left out
+template <int LAT, int i, class C>
+__device__ __forceinline__ C e_dot(C jx, C jy, C jz) {
+  using L = Lattice<LAT>;
+  C v = C(0.);
+  if constexpr (L::ex(i) == 1) v += jx;
+  if constexpr (L::ex(i) == -1) v -= jx;
+  if constexpr (L::ey(i) == 1) v += jy;
+  if constexpr (L::ey(i) == -1) v -= jy;
+  if constexpr (L::ez(i) == 1) v += jz;
+  if constexpr (L::ez(i) == -1) v -= jz;
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // MRT moment bases: rows of the non-conserved moments.
 // D2Q9: dynamics/incompressibleMRT2d.hh:50-60.  D3Q19: dynamics/MRT3d.hh:50-90.
@@ -731,7 +745,7 @@ __device__ __forceinline__ void mrt3d_pair_reverse(const C* fin, C* lam, C imult
   static_for<9>([&](auto D) {
     constexpr int d = decltype(D)::value + 1;
     const C sbar = (C(0.5) * ls[d] + rR) + gt.template G<d>();
-    C abar = C(0.5) * la[d] + (jR0 * C(L::ex(d)) + jR1 * C(L::ey(d)) + jR2 * C(L::ez(d)));
+    C abar = C(0.5) * la[d] + e_dot<LAT_D3Q19, d>(jR0, jR1, jR2);
     static_for<15>([&](auto KK) {
       constexpr int k = decltype(KK)::value;
       constexpr int c = mrt3d_m(k, d);
@@ -777,7 +791,7 @@ __device__ __forceinline__ void flow_collide(C* f, C imult, C& rho, C& jx, C& jy
       const C uSqr = jx * jx + jy * jy + jz * jz;
       static_for<L::QF>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+        const C sc = e_dot<LAT, i>(jx, jy, jz);
         C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
         f[i] = f[i] * (C(1.) - om) + om * eq;
       });
@@ -840,7 +854,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
         const C uSqr = jx * jx + jy * jy + jz * jz;
         static_for<QF>([&](auto I) {
           constexpr int i = decltype(I)::value;
-          C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+          const C sc = e_dot<LAT, i>(jx, jy, jz);
           C eq = C(L::w(i)) * (rho + C(3.) * sc + C(4.5) * sc * sc - C(1.5) * uSqr);
           fo[i] = fo[i] * (C(1.) - om) + om * eq;
         });
@@ -927,18 +941,25 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
       C rR = C(0.), jR0 = C(0.), jR1 = C(0.), jR2 = C(0.);
       static_for<QF>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        C sc = C(L::ex(i)) * jx + C(L::ey(i)) * jy + C(L::ez(i)) * jz;
+        const C sc = e_dot<LAT, i>(jx, jy, jz);
         C a = om * C(L::w(i)) * lam[i];
         rR += a;
         C ds = a * (C(3.) + C(9.) * sc);
-        jR0 += ds * C(L::ex(i)) - C(3.) * a * jx;
-        jR1 += ds * C(L::ey(i)) - C(3.) * a * jy;
-        jR2 += ds * C(L::ez(i)) - C(3.) * a * jz;
+        // jR_c += ds e_ic - 3 a j_c, the zero components of e_i left out
+        const C t3 = C(3.) * a;
+        if constexpr (L::ex(i) == 1) jR0 += ds - t3 * jx;
+        else if constexpr (L::ex(i) == -1) jR0 += -ds - t3 * jx;
+        else jR0 += -(t3 * jx);
+        if constexpr (L::ey(i) == 1) jR1 += ds - t3 * jy;
+        else if constexpr (L::ey(i) == -1) jR1 += -ds - t3 * jy;
+        else jR1 += -(t3 * jy);
+        if constexpr (L::ez(i) == 1) jR2 += ds - t3 * jz;
+        else if constexpr (L::ez(i) == -1) jR2 += -ds - t3 * jz;
+        else jR2 += -(t3 * jz);
       });
       static_for<QF>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        lam[i] = (C(1.) - om) * lam[i] + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) +
-                                          jR2 * C(L::ez(i)));
+        lam[i] = (C(1.) - om) * lam[i] + (rR + e_dot<LAT, i>(jR0, jR1, jR2));
       });
     }
   } else {
@@ -1002,7 +1023,7 @@ __device__ __forceinline__ void flow_reverse(const C* fin, C* lam, C imult, C di
           v += C(c) * a[k];
         }
       });
-      lam[i] = v + (rR + jR0 * C(L::ex(i)) + jR1 * C(L::ey(i)) + jR2 * C(L::ez(i)));
+      lam[i] = v + (rR + e_dot<LAT, i>(jR0, jR1, jR2));
     });
   }
 }
@@ -1170,19 +1191,6 @@ __device__ __forceinline__ void pair_halves(double e, double a, double& p, doubl
   m = 0.5 * (e - a);
 }
 
-// sum_a e_ia j_a with the zero terms left out
-template <int LAT, int i, class C>
-__device__ __forceinline__ C e_dot(C jx, C jy, C jz) {
-  using L = Lattice<LAT>;
-  C v = C(0.);
-  if constexpr (L::ex(i) == 1) v += jx;
-  if constexpr (L::ex(i) == -1) v -= jx;
-  if constexpr (L::ey(i) == 1) v += jy;
-  if constexpr (L::ey(i) == -1) v -= jy;
-  if constexpr (L::ez(i) == 1) v += jz;
-  if constexpr (L::ez(i) == -1) v -= jz;
-  return v;
-}
 
 // d_i -= w_i (sum d + 3 e_i . sum e d): the increments then carry no mass and
 // no momentum (sum w = 1, sum w e = 0, sum w e e = I/3).

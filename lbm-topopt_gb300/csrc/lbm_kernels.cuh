@@ -272,7 +272,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
     if constexpr (LAT == LAT_D2Q9_D2Q5) {
       static_for<9>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        d[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+        d[i] += e_dot<LAT, i>(uxR, uyR, C(0.));
       });
     }
     if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, d, dg, x, y, z, p);
@@ -316,7 +316,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
   if constexpr (LAT == LAT_D2Q9_D2Q5) {
     static_for<9>([&](auto I) {
       constexpr int i = decltype(I)::value;
-      lam[i] += uxR * C(L::ex(i)) + uyR * C(L::ey(i));
+      lam[i] += e_dot<LAT, i>(uxR, uyR, C(0.));
     });
   }
   if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p);
