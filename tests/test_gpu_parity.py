@@ -309,6 +309,19 @@ def test_errors_are_reported():
     with pytest.raises(G.LBMError) as e:
         G.Handle(bad)
     assert e.value.code == -1
+    # the largest lattice: Q * P must stay below 2^31 (32-bit population offsets);
+    # 19 x 1024 x 1024 x 128 = 2.55e9 is refused before anything is allocated
+    with pytest.raises(G.LBMError) as e:
+        G.Handle(W.duct_3d(1024, 1024, 128, storage=G.STORE_FP32))
+    assert e.value.code == G.ERR_SUP
+    # an empty horizon and a single snapshot are refused
+    with G.Handle(cfg) as h:
+        h.set_design(W.design_2d(20, 10, 1))
+        h.init_equilibrium()
+        for n, k in ((0, 8), (10, 1)):
+            with pytest.raises(G.LBMError) as e:
+                h.gradient(n, k)
+            assert e.value.code == G.ERR_ARG
 
 
 @pytest.mark.parametrize("storage", [G.STORE_FP64, G.STORE_FP32])
