@@ -535,9 +535,10 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   h->ncell = (int64_t)c.nx * c.ny * h->cfg.nz;
   h->P = (h->ncell + 127) / 128 * 128;
   if ((int64_t)h->Q * h->P >= (int64_t)INT32_MAX) {
+    const long long ncell = (long long)h->ncell;
     delete h;
     return fail(nullptr, LBM_ERR_SUP, "lattice of %lld cells too large for 32-bit population offsets",
-                (long long)h->ncell);
+                ncell);
   }
   h->pop_bytes = c.storage == LBM_STORE_FP64 ? 8 : c.storage == LBM_STORE_FP32 ? 4 : 2;
   h->adj_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
@@ -546,9 +547,10 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
               : c.lattice == LBM_D3Q19 ? launcher_d3q19(c.collision, c.storage)
                                        : launcher_thermal(c.collision, c.storage);
   if (!h->launch) {
+    const int lat = c.lattice, coll = c.collision, stor = c.storage;   // c is h->cfg
     delete h;
-    return fail(nullptr, LBM_ERR_SUP, "no kernel for lattice %d collision %d storage %d",
-                c.lattice, c.collision, c.storage);
+    return fail(nullptr, LBM_ERR_SUP, "no kernel for lattice %d collision %d storage %d", lat, coll,
+                stor);
   }
   // thread blocks: 256 threads, x-major rows
   int bx = c.nx >= 256 ? 256 : ((c.nx + 31) / 32) * 32;
@@ -567,12 +569,13 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
 
 #define ALLOC(ptr, bytes)                                                                  \
   do {                                                                                     \
-    cudaError_t ee = cudaMalloc((void**)&(ptr), (bytes));                                  \
+    const size_t nbytes_ = (bytes);                                                        \
+    cudaError_t ee = cudaMalloc((void**)&(ptr), nbytes_);                                  \
     if (ee != cudaSuccess) {                                                               \
       destroy_buffers(h);                                                                  \
       delete h;                                                                            \
       return fail(nullptr, ee == cudaErrorMemoryAllocation ? LBM_ERR_MEM : LBM_ERR_CUDA,   \
-                  "cudaMalloc(%zu bytes): %s", (size_t)(bytes), cudaGetErrorString(ee));    \
+                  "cudaMalloc(%zu bytes): %s", nbytes_, cudaGetErrorString(ee));           \
     }                                                                                      \
   } while (0)
 
