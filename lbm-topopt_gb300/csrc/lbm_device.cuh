@@ -1167,10 +1167,28 @@ struct Round<__half> {
     const float bin = fmaxf(pow2_floor(s), 6.103515625e-05f);
     return __float2half_rn(fmaf(rnd.next<10>(), bin, s));
   }
+  // Two populations from one draw (Dither::raw_pair), in packed FP32x2
+  // arithmetic with one packed conversion where the GPU has them; the same
+  // values either way.
   __device__ static __forceinline__ void apply_pair(float fa, float fb, float da, float db,
                                                     Dither& rnd, __half& oa, __half& ob) {
-    oa = apply(fa, da, rnd);
-    ob = apply(fb, db, rnd);
+    constexpr float kHalf = 1.5f / (float)(1u << 10);
+    constexpr float kSub = 6.103515625e-05f;
+    float ua, ub;
+    rnd.raw_pair<10>(ua, ub);
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    const float2 sv = __fadd2_rn(make_float2(fa, fb), make_float2(da, db));
+    const float2 u = __fadd2_rn(make_float2(ua, ub), make_float2(-kHalf, -kHalf));
+    const float2 bin = make_float2(fmaxf(pow2_floor(sv.x), kSub), fmaxf(pow2_floor(sv.y), kSub));
+    const float2 r = __ffma2_rn(u, bin, sv);
+    const __half2 h = __floats2half2_rn(r.x, r.y);
+    oa = __low2half(h);
+    ob = __high2half(h);
+#else
+    const float sa = fa + da, sb = fb + db;
+    oa = __float2half_rn(fmaf(ua - kHalf, fmaxf(pow2_floor(sa), kSub), sa));
+    ob = __float2half_rn(fmaf(ub - kHalf, fmaxf(pow2_floor(sb), kSub), sb));
+#endif
   }
 };
 

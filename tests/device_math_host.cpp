@@ -277,16 +277,24 @@ void dev_mrt3d_rows_t(const double* m, double* out) {
     out[d] = gt.template G<d>();
   });
 }
-// Round<float>::apply_pair of (f, d) twice per cell for n cells: out[2i] and
-// out[2i+1] are the two stored values of cell i.
-void dev_round_pair(float f, float d, int n, unsigned step, double* out) {
+// Round<S>::apply_pair of (f, d) twice per cell for n cells (S = __half when
+// half != 0, else float): out[2i] and out[2i+1] are the two stored values of
+// cell i.
+void dev_round_pair(int half, float f, float d, int n, unsigned step, double* out) {
   const unsigned key = step_key(step, kSaltForward);
   for (int i = 0; i < n; ++i) {
     Dither rnd((unsigned)i, key);
-    float a, b;
-    Round<float>::apply_pair(f, f, d, d, rnd, a, b);
-    out[2 * i] = (double)a;
-    out[2 * i + 1] = (double)b;
+    if (half) {
+      __half a, b;
+      Round<__half>::apply_pair(f, f, d, d, rnd, a, b);
+      out[2 * i] = (double)__half2float(a);
+      out[2 * i + 1] = (double)__half2float(b);
+    } else {
+      float a, b;
+      Round<float>::apply_pair(f, f, d, d, rnd, a, b);
+      out[2 * i] = (double)a;
+      out[2 * i + 1] = (double)b;
+    }
   }
 }
 int dev_collide(const lbm_config* c, int fp32, const double* fin, double g, double* fout) {

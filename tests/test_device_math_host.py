@@ -50,7 +50,7 @@ def devmath():
     lib.dev_round.restype = None
     lib.dev_bp.argtypes = [C.c_int, C.c_double, C.c_double, dp]
     lib.dev_bp.restype = None
-    lib.dev_round_pair.argtypes = [C.c_float, C.c_float, C.c_int, C.c_uint, dp]
+    lib.dev_round_pair.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round_pair.restype = None
     ip = C.POINTER(C.c_int)
     lib.dev_mrt3d_table.argtypes = [ip, ip]
@@ -214,21 +214,25 @@ def test_porosity_interpolation(devmath):
             assert abs((hi[0] - lo[0]) / 2e-6 - ref[1]) < 1e-6 * abs(ref[1])
 
 
-def test_pair_rounding_is_unbiased_and_uncorrelated(devmath):
-    """Round<float>::apply_pair draws the noise of two populations from one
-    step of the sequence: each output takes one of the two neighbours of
-    f + d with mean f + d, and the two rounding errors of a cell are nearly
-    uncorrelated over the cells."""
+@pytest.mark.parametrize("half", [0, 1])
+def test_pair_rounding_is_unbiased_and_uncorrelated(devmath, half):
+    """Round<S>::apply_pair draws the noise of two populations from one step
+    of the sequence: each output takes one of the two neighbours of f + d
+    with mean f + d, and the two rounding errors of a cell are nearly
+    uncorrelated over the cells (FP32 and FP16 storage)."""
     n = 200000
     out = np.zeros(2 * n)
     dp = C.POINTER(C.c_double)
-    for f, d in ((0.0123456, 3.1e-7), (-0.0071, 2.2e-6), (0.3, -1.3e-8)):
-        devmath.dev_round_pair(f, d, n, 4321, out.ctypes.data_as(dp))
+    dt = np.float16 if half else np.float32
+    cases = ((0.0123456, 3.1e-7), (-0.0071, 2.2e-6), (0.3, -1.3e-8)) if not half else \
+        ((0.0123456, 3.1e-6), (-0.0071, 2.2e-6), (0.3, -1.3e-5))
+    for f, d in cases:
+        devmath.dev_round_pair(half, f, d, n, 4321, out.ctypes.data_as(dp))
         x = float(np.float32(f)) + float(np.float32(d))
-        lo = float(np.float32(x))
+        lo = float(dt(x))
         if lo > x:
-            lo = float(np.nextafter(np.float32(x), np.float32(-np.inf)))
-        hi = float(np.nextafter(np.float32(lo), np.float32(np.inf)))
+            lo = float(np.nextafter(dt(x), dt(-np.inf)))
+        hi = float(np.nextafter(dt(lo), dt(np.inf)))
         ulp = hi - lo
         a, b = out[0::2], out[1::2]
         for v in (a, b):
