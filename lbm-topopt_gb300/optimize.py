@@ -15,6 +15,14 @@ projection sharpness rises by 1.5x every 50 iterations up to iteration 500
 (increaseBeta), and the loop stops when the design changes by less than
 1e-4.  Designs are written as PETSc binary Vec files and the fields of
 realisation 0 as .vts every --every iterations.
+
+Under torchrun (several ranks, one GPU each) the realisations are split over
+the ranks as MPISplit splits them over communicators (robustPump2d.cc:140-146):
+rank k computes the gradients of realisations r = k, k + N, ...; one sum over
+the ranks assembles every (J_r, dJ_r/dgamma) on every rank, and every rank
+takes the same (deterministic) MMA step, so the designs stay identical.
+
+    torchrun --nproc-per-node 3 --master-addr 127.0.0.1 lbm-topopt_gb300/optimize.py --robust
 """
 import argparse
 import json
@@ -44,33 +52,66 @@ def make_problem(nx, ny, nsteps, robust, storage):
     return cfg, box, stages, etas
 
 
+def owned_realisations(nreal, rank, world):
+    """The realisations rank `rank` of `world` computes: r = rank, rank + world, ..."""
+    return [r for r in range(nreal) if r % world == rank]
+
+
+def exchange_realisations(nreal, ncells, local, group=None):
+    """(J_r, dJ_r/dgamma) of every realisation on every rank.  `local` maps this
+    rank's realisations to theirs; each rank fills its own rows of a zero
+    (nreal, 1 + ncells) FP64 block and one sum over the ranks assembles the
+    block (every row has a single nonzero contributor, so the sum is exact)."""
+    import torch
+    import torch.distributed as td
+    buf = torch.zeros(nreal, ncells + 1, dtype=torch.float64)
+    for r, (J, s) in local.items():
+        buf[r, 0] = float(J)
+        buf[r, 1:] = torch.from_numpy(np.ascontiguousarray(s, dtype=np.float64))
+    td.all_reduce(buf, op=td.ReduceOp.SUM, group=group)
+    return [(float(buf[r, 0]), buf[r, 1:].numpy().copy()) for r in range(nreal)]
+
+
 def optimise(nx=256, ny=128, nsteps=2000, iters=100, robust=False, volume=0.6, nsnap=10,
-             storage=G.STORE_FP32, out_dir=None, every=50, tol=1e-4, log=print):
+             storage=G.STORE_FP32, out_dir=None, every=50, tol=1e-4, log=print,
+             rank=0, world=1, group=None):
     cfg, box, stages, etas = make_problem(nx, ny, nsteps, robust, storage)
     nreal = len(etas)
     nb = (box[1] - box[0] + 1) * (box[3] - box[2] + 1)
+    mine = owned_realisations(nreal, rank, world)
+    if not mine:
+        raise ValueError("rank %d of %d has no realisation (%d realisations)" % (rank, world, nreal))
     history = []
     with G.TopOpt(nx, ny, 1, box, stages, nreal=nreal, real_eta=etas if robust else None,
                   volume_type=G.VOLUME_FLUID, volume=volume, move_limit=0.1,
-                  x0=np.full(nb, volume)) as t, G.Batch([cfg] * nreal) as b:
+                  x0=np.full(nb, volume)) as t, G.Batch([cfg] * len(mine)) as b:
         beta = stages[-1][2]
         for it in range(iters):
             t0 = time.perf_counter()
-            for r in range(nreal):
-                t.apply(r, b[r])
-            J, _, _ = b.gradient(nsteps, nsnap, use_graph=True, schedule=G.SCHEDULE_STATIC)
-            for r in range(nreal):
-                t.set_sensitivity(r, b[r], J[r])
+            for i, r in enumerate(mine):
+                t.apply(r, b[i])
+            J, sens, _ = b.gradient(nsteps, nsnap, use_graph=True, schedule=G.SCHEDULE_STATIC)
+            if world == 1:
+                for r in range(nreal):
+                    t.set_sensitivity(r, b[r], J[r])
+            else:
+                every_r = exchange_realisations(nreal, cfg.ncells,
+                                                {r: (J[i], sens[i]) for i, r in enumerate(mine)},
+                                                group)
+                J = [Jr for Jr, _ in every_r]
+                for r, (Jr, sr) in enumerate(every_r):
+                    t.set_sensitivity_host(r, sr, Jr)
             ch, cons = t.update()
             dt = time.perf_counter() - t0
             rec = {"iteration": it, "J": [float(v) for v in J], "volume": float(cons[-1]),
                    "change": ch, "seconds": dt}
             history.append(rec)
-            log(json.dumps(rec))
-            if out_dir and (it % every == 0 or ch < tol or it == iters - 1):
+            if rank == 0:
+                log(json.dumps(rec))
+            if rank == 0 and out_dir and (it % every == 0 or ch < tol or it == iters - 1):
                 os.makedirs(out_dir, exist_ok=True)
                 G.write_petsc_vec(os.path.join(out_dir, "design_iter_%d.bin" % it), t.variables())
-                b[0].write_vts(os.path.join(out_dir, "fields_iter_%d.vts" % it), t.physical(0))
+                b[0].write_vts(os.path.join(out_dir, "fields_iter_%d.vts" % it), t.physical(mine[0]))
             if (it + 1) % 50 == 0 and it + 1 <= 500:
                 beta *= 1.5
                 t.set_beta(len(stages) - 1, beta)
@@ -92,8 +133,23 @@ def main():
     ap.add_argument("--out", default=None, help="folder for designs and .vts fields")
     ap.add_argument("--every", type=int, default=50)
     a = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    group = None
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")   # host-side exchange of the realisations' results
+        import torch
+        ndev = max(1, torch.cuda.device_count())
+        # one GPU per rank; ranks beyond the GPU count share them (their
+        # kernels never wait on one another)
+        G.select_device(int(os.environ.get("LOCAL_RANK", "0")) % ndev)
+        group = td.group.WORLD
     optimise(a.nx, a.ny, a.steps, a.iters, a.robust, a.volume,
-             storage=G.STORE_FP64 if a.fp64 else G.STORE_FP32, out_dir=a.out, every=a.every)
+             storage=G.STORE_FP64 if a.fp64 else G.STORE_FP32, out_dir=a.out, every=a.every,
+             rank=rank, world=world, group=group)
+    if world > 1:
+        td.destroy_process_group()
 
 
 if __name__ == "__main__":

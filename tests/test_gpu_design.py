@@ -164,3 +164,32 @@ def test_robust_minmax_loop(tmp_path):
     assert "design_iter_0.bin" in files and "fields_iter_0.vts" in files
     v = G.read_petsc_vec(str(tmp_path / "design_iter_0.bin"))
     assert v.size == x.size
+
+
+def test_robust_loop_split_over_two_ranks_matches_one(tmp_path):
+    """optimize.py under torchrun with two ranks (both on this GPU: their
+    kernels are independent): rank 0 computes realisations 0 and 2, rank 1
+    realisation 1, one sum over the ranks assembles all three, and every
+    rank takes the same MMA step.  The design after three iterations equals
+    the one-rank run's."""
+    import socket
+    import subprocess
+    import sys
+    import optimize as O
+    x1, _ = O.optimise(64, 32, 60, iters=3, robust=True, volume=0.6, nsnap=10,
+                       out_dir=str(tmp_path / "one"), every=100, log=lambda s: None)
+    sock = socket.socket()
+    sock.bind(("127.0.0.1", 0))
+    port = sock.getsockname()[1]
+    sock.close()
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = os.path.join(os.path.dirname(here), "lbm-topopt_gb300", "optimize.py")
+    out = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                          "--nproc-per-node=2", "--master-addr=127.0.0.1", "--master-port=%d" % port,
+                          script, "--robust", "--nx", "64", "--ny", "32", "--steps", "60",
+                          "--iters", "3", "--every", "100", "--out", str(tmp_path / "two")],
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    x2 = G.read_petsc_vec(str(tmp_path / "two" / "design_iter_2.bin"))
+    assert x2.size == x1.size
+    assert np.abs(x2 - x1).max() <= 1e-12

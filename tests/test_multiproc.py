@@ -1,6 +1,8 @@
-"""The N-GPU bench path on CPU: two gloo ranks run the replica reduction of
+"""The multi-rank paths on CPU with two gloo ranks: the replica reduction of
 bench.py (barrier, max over ranks of the device time, sum of the lattice
-updates), and the reference arm prints from rank 0 only."""
+updates), the reference arm printing from rank 0 only, and the split of the
+robust realisations over ranks in optimize.py (each rank computes its own
+realisations; one sum assembles every (J_r, dJ_r/dgamma) on every rank)."""
 import os
 import socket
 import subprocess
@@ -57,3 +59,44 @@ def test_reference_arm_prints_on_rank0_only():
                          timeout=300)
     assert out.returncode == 0
     assert out.stdout.strip() == ""
+
+
+def _robust_worker(rank, world, port, nreal, ncells, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    sys.path.insert(0, os.path.join(ROOT, "lbm-topopt_gb300"))
+    import numpy as np
+    import torch.distributed as td
+    import optimize as O
+    td.init_process_group("gloo")
+    mine = O.owned_realisations(nreal, rank, world)
+    # realisation r's stand-in results: J_r = r + 0.25, dJ_r/dgamma = (r + 1) * [1, 2, ...] / 7
+    local = {r: (r + 0.25, (r + 1) * np.arange(1, ncells + 1) / 7.0) for r in mine}
+    full = O.exchange_realisations(nreal, ncells, local)
+    q.put((rank, mine, [J for J, _ in full], [s.tolist() for _, s in full]))
+    td.destroy_process_group()
+
+
+def test_robust_realisations_split_over_two_gloo_ranks():
+    torch = pytest.importorskip("torch")
+    import numpy as np
+    mp = torch.multiprocessing.get_context("spawn")
+    q = mp.Queue()
+    port = _free_port()
+    nreal, ncells = 3, 37
+    procs = [mp.Process(target=_robust_worker, args=(r, 2, port, nreal, ncells, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    # every realisation is computed by exactly one rank
+    owned = [r for _, mine, _, _ in res for r in mine]
+    assert sorted(owned) == list(range(nreal))
+    assert res[0][1] == [0, 2] and res[1][1] == [1]
+    # and every rank ends with the same, exact results of all of them
+    for _, _, Js, ss in res:
+        assert Js == [r + 0.25 for r in range(nreal)]
+        for r in range(nreal):
+            assert np.array_equal(np.array(ss[r]), (r + 1) * np.arange(1, ncells + 1) / 7.0)
