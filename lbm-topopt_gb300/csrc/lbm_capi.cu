@@ -80,7 +80,7 @@ struct lbm_handle {
   float* bcprof_f[LBM_MAX_BC] = {};
   int t = 0;
   bool have_design = false, have_state = false, have_adjoint = false;
-  bool accumulate = false;   // objective sums over steps into the block partials
+  bool accumulate = false;   // objective sums over steps into the warp partials
   int64_t launches = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::string err;
@@ -965,7 +965,7 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
     if ((rc = init_into(h, pool_buffer(h, out)))) return rc;
     pool.set_current(out);
   }
-  // J = sum_t F(f_t), summed in the block partials across the sweep
+  // J = sum_t F(f_t), summed in the warp partials across the sweep
   if (obj && (rc = begin_accumulate(h))) return rc;
   if ((rc = save(place(0)))) {
     h->accumulate = false;
@@ -1446,7 +1446,7 @@ int batch_sequence(lbm_batch* b, int nsteps, int nsnap, int schedule, int64_t* r
     if ((rc = batch_init(b, out))) return rc;
     pool.set_current(out);
   }
-  // J of every lattice summed in its block partials across the sweep
+  // J of every lattice summed in its warp partials across the sweep
   for (int i = 0; i < b->n; ++i)
     if (b->h[i]->cfg.objective != LBM_OBJ_NONE && (rc = begin_accumulate(b->h[i], b->stream)))
       return bfail(b, rc, "%s", b->h[i]->err.c_str());

@@ -229,7 +229,7 @@ struct KParams {
   int accumulate;          // add each block's sum to partial[block] (no counter, no result)
   double obj_weight, inv_in, inv_out;
   int obj_in[6], obj_out[6];
-  double* partial;         // per-block partial sums
+  double* partial;         // partial sums: per block (one step) or per warp (summed over steps)
   unsigned int* counter;   // last-block-done counter (reset by the last block)
   double* result;          // J of this step (written by the last block)
   // buffers
