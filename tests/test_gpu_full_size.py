@@ -8,7 +8,9 @@ horizon.
   oracle within 1e-12 at the sizes the oracle runs): J within 1e-6 and
   dJ/dgamma within 1e-5 (relative L2).
 * A repeated gradient is bit-identical (rounding streams are keyed by cell
-  and step, not by launch order)."""
+  and step, not by launch order).
+* The FP64 gradient agrees with central differences (h = 1e-6) of the FP64
+  objective at the four cells of largest sensitivity."""
 import numpy as np
 import pytest
 
@@ -54,3 +56,23 @@ def test_full_size_fp32_against_fp64(duct):
     e = rel_l2(s32, s64)
     print("full-size 200-step FP32 vs FP64: J %.3e, dJ/dgamma %.3e" % (abs(J32 - J64) / abs(J64), e))
     assert e < 1e-5
+
+
+def test_full_size_fp64_gradient_matches_central_differences(duct):
+    cfg, gamma = duct
+    cfg = cfg.replace(storage=G.STORE_FP64)
+    J, sens, _ = gradient(cfg, gamma, 16)
+    cells = np.argsort(-np.abs(sens))[:4]
+    h = 1e-6
+    with G.Handle(cfg) as hd:
+        for c in cells:
+            vals = []
+            for sg in (1, -1):
+                g = gamma.copy()
+                g[c] = min(1.0, max(0.0, g[c] + sg * h))
+                hd.set_design(g)
+                hd.init_equilibrium()
+                vals.append((hd.forward(N), g[c]))
+            fd = (vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1])
+            print("cell %d: adjoint %.6e, central difference %.6e" % (c, sens[c], fd))
+            assert abs(fd - sens[c]) <= 1e-4 * abs(sens[c])
