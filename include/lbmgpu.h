@@ -309,8 +309,8 @@ int lbm_schedule_count(int nsteps, int nsnapshots, int schedule, int64_t* recomp
 /* ------------------------------------------------------------------------
  * Batches.  Up to LBM_MAX_BATCH lattices with the same lattice type, collision
  * and storage (sizes, boundaries, designs and objectives free) advanced
- * together: one launch per time step covers every lattice, a persistent grid of
- * resident blocks striding over their concatenated blocks.  The one-GPU form of
+ * together: one launch per time step covers every lattice, its blocks laid
+ * over their concatenated blocks.  The one-GPU form of
  * the reference's robust-design ensembles (core/MPISplit.cc:14-59,
  * applications/RobustPump2d/robustPump2d.cc:140-146), where each realisation
  * ran on its own MPI sub-communicator. */

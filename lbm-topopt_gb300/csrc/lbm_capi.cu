@@ -1272,7 +1272,15 @@ dim3 batch_block(const lbm_batch* b, int kind) {
   return (kind == K_ADJOINT || kind == K_ADJOINT_LEAN) ? dim3(b->abx, b->aby) : dim3(b->bx, b->by);
 }
 
+// Grid of a batched kernel over `total` virtual blocks.  The step kernels get
+// one CTA per virtual block, as a single lattice's launch does, so that
+// programmatic dependent launch can schedule the next step's CTAs into the
+// previous step's last wave (a resident-CTA grid striding over the virtual
+// blocks cannot: 8 D2Q9 lattices of config 5 took 43.2 / 64.9 us per forward
+// / reverse step that way, 38.8 / 62.0 us now).  The objective kernel keeps
+// a grid of resident CTAs striding over the blocks.
 int batch_grid(lbm_batch* b, int kind, int total) {
+  if (kind == K_FORWARD || kind == K_ADJOINT || kind == K_ADJOINT_LEAN) return total;
   int per_sm = 1;
   const void* k = b->ops.kernel(kind);
   const dim3 blk = batch_block(b, kind);

@@ -400,9 +400,10 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
 // ---------------------------------------------------------------------------
 // Batched kernels: one launch advances every lattice of a batch (uneven sizes,
 // each with its own boundaries, design and objective).  The virtual blocks of
-// all lattices are concatenated; a persistent grid of resident blocks strides
-// over them, so small and large lattices share the SMs.  Per-lattice
-// parameters are read in place from the launch's parameter space.
+// all lattices are concatenated and the grid strides over them (the step
+// kernels are launched with one block per virtual block, the objective kernel
+// with the resident blocks), so small and large lattices share the SMs.
+// Per-lattice parameters are read in place from the launch's parameter space.
 
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
