@@ -1298,6 +1298,11 @@ void batch_layout(lbm_batch* b, BatchParams& bp, int kind) {
     const lbm_handle* h = b->h[i];
     bp.gx[i] = (h->cfg.nx + (int)blk.x - 1) / (int)blk.x;
     bp.gy[i] = (h->cfg.ny + (int)blk.y - 1) / (int)blk.y;
+    // multiply-high divisors (batch_div): the numerators stay below the
+    // lattice's block count gx*gy*nz (for gx) and gy*nz (for gy)
+    const uint64_t nblk = (uint64_t)bp.gx[i] * bp.gy[i] * h->cfg.nz;
+    bp.gxm[i] = batch_div_magic((uint64_t)bp.gx[i], nblk);
+    bp.gym[i] = batch_div_magic((uint64_t)bp.gy[i], nblk / (uint64_t)bp.gx[i]);
     bp.start[i] = start;
     start += bp.gx[i] * bp.gy[i] * h->cfg.nz;
   }

@@ -1928,7 +1928,26 @@ struct BatchParams {
   int n;                        // lattices in the batch
   int start[kMaxBatch + 1];     // first virtual block of each lattice; start[n] = total
   int gx[kMaxBatch], gy[kMaxBatch];   // blocks along x and y of each lattice (z: one per plane)
+  // ceil(2^32 / gx) and ceil(2^32 / gy) for batch_div, or 0 where the
+  // multiply-high form does not apply (a divisor of 1, or a product n * d
+  // that can reach 2^32)
+  unsigned gxm[kMaxBatch], gym[kMaxBatch];
   KParams p[kMaxBatch];
 };
+
+// n / d by a multiply-high with m = ceil(2^32 / d): with 2^32 + e = m d
+// (0 <= e < d) and n = q d + r, n m / 2^32 = q + r / d + n e / (d 2^32), whose
+// floor is q whenever n e < 2^32, so whenever n d < 2^32.  m = 0 falls back
+// to the division.
+__device__ __forceinline__ unsigned batch_div(unsigned n, unsigned d, unsigned m) {
+  return m ? __umulhi(n, m) : n / d;
+}
+
+// The m of batch_div: ceil(2^32 / d) when every numerator n < nmax gives
+// n * d < 2^32 and d > 1, else 0.
+__host__ __device__ inline unsigned batch_div_magic(unsigned long long d, unsigned long long nmax) {
+  if (d < 2 || nmax * d >= (1ull << 32)) return 0u;
+  return (unsigned)(((1ull << 32) + d - 1) / d);
+}
 
 }  // namespace lbm

@@ -414,10 +414,11 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
-    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
-    const int x = bx * blockDim.x + threadIdx.x;
-    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
-    const auto objv = forward_cell<LAT, COLL, S>(p, x, y, r / bp.gy[i]);
+    const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
+    const int bz = (int)batch_div((unsigned)r, (unsigned)bp.gy[i], bp.gym[i]);
+    const int x = (lb - r * bp.gx[i]) * blockDim.x + threadIdx.x;
+    const int y = (r - bz * bp.gy[i]) * blockDim.y + threadIdx.y;
+    const auto objv = forward_cell<LAT, COLL, S>(p, x, y, bz);
     if (p.eval_obj) grid_reduce_v(objv, p, lb, bp.start[i + 1] - bp.start[i]);
   }
 }
@@ -432,10 +433,11 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
     while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
-    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
-    const int x = bx * blockDim.x + threadIdx.x;
-    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
-    adjoint_cell<LAT, COLL, S>(p, x, y, r / bp.gy[i]);
+    const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
+    const int bz = (int)batch_div((unsigned)r, (unsigned)bp.gy[i], bp.gym[i]);
+    const int x = (lb - r * bp.gx[i]) * blockDim.x + threadIdx.x;
+    const int y = (r - bz * bp.gy[i]) * blockDim.y + threadIdx.y;
+    adjoint_cell<LAT, COLL, S>(p, x, y, bz);
   }
 }
 
@@ -446,10 +448,11 @@ __global__ void __launch_bounds__(256) k_objective_batch(const __grid_constant__
     while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
-    const int bx = lb % bp.gx[i], r = lb / bp.gx[i];
-    const int x = bx * blockDim.x + threadIdx.x;
-    const int y = (r % bp.gy[i]) * blockDim.y + threadIdx.y;
-    const auto v = objective_only_cell<LAT, S>(p, x, y, r / bp.gy[i]);
+    const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
+    const int bz = (int)batch_div((unsigned)r, (unsigned)bp.gy[i], bp.gym[i]);
+    const int x = (lb - r * bp.gx[i]) * blockDim.x + threadIdx.x;
+    const int y = (r - bz * bp.gy[i]) * blockDim.y + threadIdx.y;
+    const auto v = objective_only_cell<LAT, S>(p, x, y, bz);
     if (p.eval_obj) grid_reduce_v(v, p, lb, bp.start[i + 1] - bp.start[i]);
   }
 }

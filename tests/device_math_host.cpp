@@ -22,6 +22,7 @@ inline int __syncthreads_or(int v) { return v; }
 inline void __threadfence() {}
 inline unsigned atomicAdd(unsigned* p, unsigned v) { unsigned o = *p; *p += v; return o; }
 inline double atomicAdd(double* p, double v) { double o = *p; *p += v; return o; }
+inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 inline float __ldcs(const float* p) { return *p; }
 inline void __stcs(float* p, float v) { *p = v; }
 inline float __uint_as_float(unsigned u) { float f; memcpy(&f, &u, 4); return f; }
@@ -267,6 +268,13 @@ void dev_bp(int fp32, double s, double q, double* out) {
     out[0] = bp<double>(s, q);
     out[1] = bp_diff<double>(s, q);
   }
+}
+// batch_div(n, d, batch_div_magic(d, nmax)) for the batch layout.
+unsigned dev_batch_div(unsigned n, unsigned d, unsigned long long nmax) {
+  return batch_div(n, d, batch_div_magic(d, nmax));
+}
+unsigned dev_batch_div_magic(unsigned long long d, unsigned long long nmax) {
+  return batch_div_magic(d, nmax);
 }
 // Transposed even rows for moment adjoints m: G_0, then G_d for d = 1..9.
 void dev_mrt3d_rows_t(const double* m, double* out) {

@@ -48,6 +48,10 @@ def devmath():
     lib.dev_reverse_inc.argtypes = [C.POINTER(G.CConfig), C.c_int, dp, C.c_double, dp, dp, dp]
     lib.dev_round.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
     lib.dev_round.restype = None
+    lib.dev_batch_div.argtypes = [C.c_uint, C.c_uint, C.c_ulonglong]
+    lib.dev_batch_div.restype = C.c_uint
+    lib.dev_batch_div_magic.argtypes = [C.c_ulonglong, C.c_ulonglong]
+    lib.dev_batch_div_magic.restype = C.c_uint
     lib.dev_bp.argtypes = [C.c_int, C.c_double, C.c_double, dp]
     lib.dev_bp.restype = None
     lib.dev_round_pair.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_uint, dp]
@@ -187,6 +191,23 @@ def test_stochastic_rounding_is_unbiased(devmath, half):
         x = float(np.float32(f)) + float(np.float32(d))
         ulp_lo = float(np.spacing(dt(min(abs(x), f) * 0.999)))
         assert abs(out.mean() - x) < 0.25 * ulp_lo, (f, d, (out.mean() - x) / ulp_lo)
+
+
+def test_batch_block_division(devmath):
+    """The batched kernels split a virtual block index with a multiply-high
+    by ceil(2^32 / d), exact while n * d < 2^32; outside that bound (and for
+    d = 1) the magic number is 0 and the kernel divides."""
+    rng = np.random.default_rng(9)
+    for d in list(range(1, 300)) + [int(v) for v in rng.integers(2, 1 << 16, 300)]:
+        nmax = (1 << 32) // d
+        m = devmath.dev_batch_div_magic(d, nmax)
+        assert (m == 0) == (d == 1 or nmax * d >= (1 << 32))
+        if d > 1:
+            assert devmath.dev_batch_div_magic(d, nmax - 1) != 0
+        lim = min(nmax - 1, (1 << 32) - 1)
+        for n in [0, 1, d - 1, d, d + 1, lim, lim - d, lim // 2] + [int(v) for v in rng.integers(0, lim + 1, 40)]:
+            if 0 <= n <= lim:
+                assert devmath.dev_batch_div(n, d, lim + 1) == n // d, (n, d)
 
 
 def test_porosity_interpolation(devmath):
