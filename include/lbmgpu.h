@@ -263,7 +263,8 @@ int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms);
 /* Time every candidate thread-block shape of the forward and reverse step
  * kernels (and both register variants of the reverse step) for nsteps steps
  * each on this handle's lattice and keep the fastest (the tile-shape
- * autotuner).  Needs a design and a state; the state
+ * autotuner).  Forward steps are timed with the objective summed over the
+ * steps, as a gradient's forward sweep runs them.  Needs a design and a state; the state
  * is left unchanged and the adjoint and sensitivity fields are zeroed. */
 int lbm_autotune(lbm_handle* h, int nsteps);
 

@@ -1071,6 +1071,12 @@ int lbm_autotune(lbm_handle* h, int nsteps) {
   bool blean = h->adj_lean;
   const int nx = h->cfg.nx;
   const int nlean = h->cfg.storage == LBM_STORE_FP64 ? 1 : 2;   // FP64 has no lean variant
+  // Forward steps are timed as a gradient's forward sweep runs them, with the
+  // objective summed into the warp partials (scratch here; the next sweep
+  // zeroes them): the shapes differ most in that reduction.
+  const bool obj = h->cfg.objective != LBM_OBJ_NONE;
+  if (obj && (rc = ensure_jcap(h, 1))) { cudaFree(keep); return rc; }
+  double* jres = obj ? h->jdev : nullptr;
   for (const auto& sh : kShapes) {
     if (sh[0] > ((nx + 31) / 32) * 32 && sh[0] > 32) continue;
     Geometry g = make_geometry(nx, h->cfg.ny, h->cfg.nz, sh[0], sh[1]);
@@ -1078,12 +1084,14 @@ int lbm_autotune(lbm_handle* h, int nsteps) {
       // which: 0 forward, 1 reverse, 2 reverse (lean variant)
       (which == 0 ? h->geo_fwd : h->geo_adj) = g;
       if (which >= 1) h->adj_lean = which == 2;
+      h->accumulate = which == 0 && obj;
       // one untimed launch, then nsteps timed
-      rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
-      if (rc) { cudaFree(keep); return rc; }
+      rc = which == 0 ? forward_step(h, jres) : adjoint_step(h);
+      if (rc) { h->accumulate = false; cudaFree(keep); return rc; }
       cudaEventRecord(h->ev[0], h->stream);
-      for (int k = 0; k < nsteps && !rc; ++k) rc = which == 0 ? forward_step(h, nullptr) : adjoint_step(h);
+      for (int k = 0; k < nsteps && !rc; ++k) rc = which == 0 ? forward_step(h, jres) : adjoint_step(h);
       cudaEventRecord(h->ev[1], h->stream);
+      h->accumulate = false;
       if (rc || (rc = sync(h))) { cudaFree(keep); return rc; }
       float ms = 0.f;
       cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
@@ -1610,6 +1618,18 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
   int fbx = b->bx, fby = b->by, abx = b->abx, aby = b->aby;
   bool alean = b->adj_lean;
   const int nlean = b->h[0]->cfg.storage == LBM_STORE_FP64 ? 1 : 2;
+  // forward steps timed with the objectives summed into the warp partials, as
+  // a gradient's forward sweep runs them (the partials are scratch here)
+  double* res[LBM_MAX_BATCH] = {};
+  for (int i = 0; i < b->n; ++i) {
+    lbm_handle* h = b->h[i];
+    if (h->cfg.objective == LBM_OBJ_NONE) continue;
+    if ((rc = ensure_jcap(h, 1))) return bfail(b, rc, "%s", h->err.c_str());
+    res[i] = h->jdev;
+  }
+  auto accumulate_all = [&](bool on) {
+    for (int i = 0; i < b->n; ++i) b->h[i]->accumulate = on && res[i] != nullptr;
+  };
   for (int which = 0; which < 1 + nlean; ++which) {
     for (const auto& sh : kShapes) {
       if (which == 0) {
@@ -1621,12 +1641,17 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps) {
         b->adj_lean = which == 2;
       }
       batch_set_grids(b);
-      rc = which == 0 ? batch_forward(b, nullptr) : batch_adjoint(b, kCurState);
-      if (rc) return rc;
+      accumulate_all(which == 0);
+      rc = which == 0 ? batch_forward(b, res) : batch_adjoint(b, kCurState);
+      if (rc) {
+        accumulate_all(false);
+        return rc;
+      }
       cudaEventRecord(b->ev[0], b->stream);
       for (int k = 0; k < nsteps && !rc; ++k)
-        rc = which == 0 ? batch_forward(b, nullptr) : batch_adjoint(b, kCurState);
+        rc = which == 0 ? batch_forward(b, res) : batch_adjoint(b, kCurState);
       cudaEventRecord(b->ev[1], b->stream);
+      accumulate_all(false);
       if (rc) return rc;
       BCUDA(b, cudaStreamSynchronize(b->stream));
       float ms = 0.f;
