@@ -232,7 +232,7 @@ def cpu_model():
 
 def slab_case(nz_slab):
     import workloads as W
-    cfg, g, _ = W.workload_config3(W.STORE_FP64, nx=NX, ny=NY, nz=nz_slab, nsteps=NSTEPS_GRAD)
+    cfg, g, _ = W.workload_duct_256x128x128(W.STORE_FP64, nx=NX, ny=NY, nz=nz_slab, nsteps=NSTEPS_GRAD)
     return cfg, g
 
 
@@ -288,7 +288,7 @@ def reference_arm(args, world, rank):
 def precision_errors(G, W):
     """Population error of FP32 / FP16 storage against the FP64 path on a
     64x32x32 duct after 300 steps (the FP64 GPU path equals the oracle to 1e-12)."""
-    cfg, g, _ = W.workload_config3(G.STORE_FP64, nx=64, ny=32, nz=32, nsteps=300)
+    cfg, g, _ = W.workload_duct_256x128x128(G.STORE_FP64, nx=64, ny=32, nz=32, nsteps=300)
     out = {}
     ref = None
     for name, st in (("fp64", G.STORE_FP64), ("fp32", G.STORE_FP32), ("fp16", G.STORE_FP16)):
@@ -323,7 +323,7 @@ def main():
     import lbmgpu as G
     import workloads as W
     G.select_device(local)
-    cfg, gamma, _ = W.workload_config3(G.STORE_FP32, nx=NX, ny=NY, nz=NZ, nsteps=NSTEPS_GRAD)
+    cfg, gamma, _ = W.workload_duct_256x128x128(G.STORE_FP32, nx=NX, ny=NY, nz=NZ, nsteps=NSTEPS_GRAD)
     cells = cfg.ncells
     h = G.Handle(cfg)
     h.set_design(gamma)

@@ -1,25 +1,27 @@
-"""Measurements of the five workloads on the GPU, one JSON line each.
+"""Measurements of the six workloads on the GPU, one JSON line each.
 
-    python lbm-topopt_gb300/report.py [--configs 1 2 3 4 5] [--quick]
+    python lbm-topopt_gb300/report.py [--workloads channel duct ...] [--quick]
 
-1  128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps: forward and gradient time,
-   agreement with the FP64 oracle.
-2  1024x512 D2Q9, unsteady inlet, dissipated energy, 20000 steps with 64
-   device snapshots: gradient wall time FP64 vs FP32 shifted storage, FP32
-   error against FP64, dJ/dgamma against central differences (h = 1e-6, FP64)
-   at 16 seeded cells on a 2000-step horizon (one inlet period), and against
-   the reference adjoint (the oracle, bit-identical to the reference's own
-   operators) on a 128x64 cut-down.
-3  256x128x128 D3Q19 MRT duct: FP64 / FP32 / FP16 storage MLUPS and errors
-   (bench.py measures its FP32 headline).
-4  512x256 D2Q9 + D2Q5 thermal, 10000 steps, FP32 with FP64 objective
-   accumulation: gradient time, error against FP64.
-5  8 D2Q9 lattices (3 projected designs of 1024x512 + 5 uneven ones), 4000
-   steps: batched gradient (one launch per step, CUDA graph) against the same
-   lattices one at a time.
-6  robust design iteration on the device: 3 realisations of the 1024x512
-   channel, double projection filter, batched gradient, chain rule and one
-   min-max MMA step, with the CPU oracle's filter and MMA beside it.
+channel           128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps: forward and
+                  gradient time, agreement with the FP64 oracle.
+unsteady_channel  1024x512 D2Q9, unsteady inlet, dissipated energy, 20000
+                  steps with 64 device snapshots: gradient wall time FP64 vs
+                  FP32 shifted storage, FP32 error against FP64, dJ/dgamma
+                  against central differences (h = 1e-6, FP64) at 16 seeded
+                  cells on a 2000-step horizon (one inlet period), and against
+                  the reference adjoint (the oracle, bit-identical to the
+                  reference's own operators) on a 128x64 cut-down.
+duct              256x128x128 D3Q19 MRT duct: FP64 / FP32 / FP16 storage MLUPS
+                  and errors (bench.py measures its FP32 headline).
+thermal           512x256 D2Q9 + D2Q5 thermal, 10000 steps, FP32 with FP64
+                  objective accumulation: gradient time, error against FP64.
+batch             8 D2Q9 lattices (3 projected designs of 1024x512 + 5 uneven
+                  ones), 4000 steps: batched gradient (one launch per step,
+                  CUDA graph) against the same lattices one at a time.
+robust            robust design iteration on the device: 3 realisations of the
+                  1024x512 channel, double projection filter, batched
+                  gradient, chain rule and one min-max MMA step, with the CPU
+                  oracle's filter and MMA beside it.
 """
 import argparse
 import json
@@ -72,8 +74,8 @@ def step_rates(cfg, gamma, nsteps=50):
     return cfg.ncells * nsteps / mf / 1e3, cfg.ncells * nsteps / ma / 1e3
 
 
-def config1(quick):
-    cfg, g, n = W.workload_config1()
+def report_channel(quick):
+    cfg, g, n = W.workload_channel_128x64()
     orc = _oracle()
     with G.Handle(cfg) as h:
         h.set_design(g)
@@ -84,19 +86,19 @@ def config1(quick):
         f = h.populations()
     fo, _, Jo = orc.forward(cfg, g, n)
     Jg, s, st, tg = timed_gradient(cfg, g, n, 64)
-    return {"config": 1, "workload": "128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps",
+    return {"workload_name": "channel", "workload": "128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps",
             "forward_s": tf, "gradient_s_64_snapshots": tg, "recomputed": st.recomputed_steps,
             "J": J, "J_rel_err_vs_oracle": abs(J - Jo) / abs(Jo),
             "populations_max_rel_err_vs_oracle": float(np.abs(f - fo).max() / np.abs(fo).max())}
 
 
-def config2(quick):
+def report_unsteady_channel(quick):
     n = 2000 if quick else 20000
-    cfg64, g, _ = W.workload_config2(G.STORE_FP64, nsteps=n)
+    cfg64, g, _ = W.workload_unsteady_channel_1024x512(G.STORE_FP64, nsteps=n)
     cfg32 = cfg64.replace(storage=G.STORE_FP32)
     J64, s64, st, t64 = timed_gradient(cfg64, g, n, 64)
     J32, s32, _, t32 = timed_gradient(cfg32, g, n, 64)
-    out = {"config": 2, "workload": "1024x512 D2Q9 BGK + Brinkman, unsteady inlet, dissipated "
+    out = {"workload_name": "unsteady_channel", "workload": "1024x512 D2Q9 BGK + Brinkman, unsteady inlet, dissipated "
                                     "energy, %d steps, 64 device snapshots" % n,
            "recomputed": st.recomputed_steps, "gradient_s_fp64": t64, "gradient_s_fp32": t32,
            "speedup_fp32": t64 / t32, "J_fp64": J64, "J_fp32_rel_err": abs(J32 - J64) / abs(J64),
@@ -125,7 +127,7 @@ def config2(quick):
     out.update(fd_cells=int(len(cells)), fd_steps=nfd, fd_h=h_fd, fd_max_err_rel_to_max_sens=worst)
     # reference adjoint on the 128x64 cut-down
     orc = _oracle()
-    ccut, gcut, _ = W.workload_config2(G.STORE_FP64, nx=128, ny=64, nsteps=2000)
+    ccut, gcut, _ = W.workload_unsteady_channel_1024x512(G.STORE_FP64, nx=128, ny=64, nsteps=2000)
     Jc, sc, _, _ = timed_gradient(ccut, gcut, 2000, 64)
     Jo, so = orc.gradient(ccut, gcut, 2000)
     out.update(cutdown_J_rel_err=abs(Jc - Jo) / abs(Jo),
@@ -133,14 +135,14 @@ def config2(quick):
     return out
 
 
-def config3(quick):
-    out = {"config": 3, "workload": "256x128x128 D3Q19 MRT + Brinkman duct"}
+def report_duct(quick):
+    out = {"workload_name": "duct", "workload": "256x128x128 D3Q19 MRT + Brinkman duct"}
     for name, st in (("fp64", G.STORE_FP64), ("fp32", G.STORE_FP32), ("fp16", G.STORE_FP16)):
-        cfg, g, _ = W.workload_config3(st)
+        cfg, g, _ = W.workload_duct_256x128x128(st)
         mf, ma = step_rates(cfg, g, 10 if st == G.STORE_FP64 else 50)
         out["mlups_fwd_" + name] = mf
         out["mlups_adj_" + name] = ma
-    cfg, g, _ = W.workload_config3(G.STORE_FP64, nx=64, ny=32, nz=32, nsteps=300)
+    cfg, g, _ = W.workload_duct_256x128x128(G.STORE_FP64, nx=64, ny=32, nz=32, nsteps=300)
     J64, s64, _, _ = timed_gradient(cfg, g, 300, 32)
     for name, st in (("fp32", G.STORE_FP32), ("fp16", G.STORE_FP16)):
         J, s, _, _ = timed_gradient(cfg.replace(storage=st), g, 300, 32)
@@ -149,22 +151,22 @@ def config3(quick):
     return out
 
 
-def config4(quick):
+def report_thermal(quick):
     n = 2000 if quick else 10000
-    cfg64, g, _ = W.workload_config4(G.STORE_FP64, nsteps=n)
+    cfg64, g, _ = W.workload_thermal_512x256(G.STORE_FP64, nsteps=n)
     cfg32 = cfg64.replace(storage=G.STORE_FP32)
     J64, s64, st, t64 = timed_gradient(cfg64, g, n, 64)
     J32, s32, _, t32 = timed_gradient(cfg32, g, n, 64)
     mf, ma = step_rates(cfg32, g)
-    return {"config": 4, "workload": "512x256 D2Q9 + D2Q5 thermal, heat flux, %d steps" % n,
+    return {"workload_name": "thermal", "workload": "512x256 D2Q9 + D2Q5 thermal, heat flux, %d steps" % n,
             "gradient_s_fp64": t64, "gradient_s_fp32": t32, "recomputed": st.recomputed_steps,
             "J_fp64": J64, "J_fp32_rel_err": abs(J32 - J64) / abs(J64),
             "dJdgamma_fp32_rel_l2_err": rel(s32, s64), "mlups_fwd_fp32": mf, "mlups_adj_fp32": ma}
 
 
-def config5(quick):
+def report_batch(quick):
     n = 400 if quick else 4000
-    insts, _ = W.workload_config5(G.STORE_FP32, nsteps=n)
+    insts, _ = W.workload_batch_8_channels(G.STORE_FP32, nsteps=n)
     cells = sum(c.ncells for c, _ in insts)
     # one at a time
     t_single = 0.0
@@ -184,7 +186,7 @@ def config5(quick):
         t0 = time.perf_counter()
         b.gradient(n, 64, use_graph=False)
         t_eager = time.perf_counter() - t0
-    return {"config": 5, "workload": "8 D2Q9 lattices (3 projected 1024x512 + 256x128 .. 768x384), "
+    return {"workload_name": "batch", "workload": "8 D2Q9 lattices (3 projected 1024x512 + 256x128 .. 768x384), "
                                      "FP32, %d steps, 64 snapshots each" % n,
             "cells": cells, "batch_block_shape": list(shape),
             "gradient_s_batched_graph": t_batch, "gradient_s_batched_no_graph": t_eager,
@@ -194,7 +196,7 @@ def config5(quick):
             "max_J_rel_diff_batched_vs_single": float(max(abs(a - b) / abs(b) for a, b in zip(J, Js)))}
 
 
-def config6(quick):
+def report_robust(quick):
     """Robust design iteration at the batch scale: three realisations (the
     second projection's eta 0.3 / 0.5 / 0.7) of the 1024x512 channel, the
     double projection filter of RobustPump2d (radii 8 and 4), one batched
@@ -213,7 +215,7 @@ def config6(quick):
     mask[box[2]:box[3] + 1, box[0]:box[1] + 1] = True
     x0 = W.design_2d(nx, ny, W.SEED_BASE + 6).reshape(ny, nx)[mask]
     x0 = np.clip(x0, 0.0, 1.0)
-    out = {"config": 6, "workload": "robust design iteration: 3 realisations of a 1024x512 D2Q9 "
+    out = {"workload_name": "robust", "workload": "robust design iteration: 3 realisations of a 1024x512 D2Q9 "
                                     "channel, double projection (R 8 + 4), FP32 gradient of %d "
                                     "steps, min-max MMA with a fluid-volume constraint" % n,
            "design_variables": int(mask.sum())}
@@ -270,15 +272,19 @@ def config6(quick):
     return out
 
 
+REPORTS = {"channel": report_channel, "unsteady_channel": report_unsteady_channel,
+           "duct": report_duct, "thermal": report_thermal, "batch": report_batch,
+           "robust": report_robust}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--configs", type=int, nargs="*", default=[1, 2, 3, 4, 5, 6])
+    ap.add_argument("--workloads", nargs="*", choices=list(REPORTS), default=list(REPORTS))
     ap.add_argument("--quick", action="store_true", help="shorter horizons")
     a = ap.parse_args()
-    fns = {1: config1, 2: config2, 3: config3, 4: config4, 5: config5, 6: config6}
-    for c in a.configs:
+    for c in a.workloads:
         t0 = time.perf_counter()
-        r = fns[c](a.quick)
+        r = REPORTS[c](a.quick)
         r["wall_s"] = time.perf_counter() - t0
         print(json.dumps(r), flush=True)
 

@@ -1,6 +1,6 @@
-"""Run forward and reverse time steps of one of the five workloads on the GPU.
+"""Run forward and reverse time steps of one of the single-lattice workloads on the GPU.
 
-    python lbm-topopt_gb300/run_steps.py --workload 3 --storage fp32 --fwd 20 --adj 20
+    python lbm-topopt_gb300/run_steps.py --workload duct --storage fp32 --fwd 20 --adj 20
 
 Prints the device time per step (CUDA events on the library's stream) and the
 MLUPS.  Small enough to run under a profiler: it launches only the forward
@@ -17,40 +17,41 @@ if HERE not in sys.path:
 import lbmgpu as G  # noqa: E402
 import workloads as W  # noqa: E402
 
+WORKLOADS = ("channel", "unsteady_channel", "duct", "thermal")
 STORAGE = {"fp64": G.STORE_FP64, "fp32": G.STORE_FP32, "fp16": G.STORE_FP16}
 
 
-def build_workload(which: int, storage: int, size=None):
+def build_workload(which: str, storage: int, size=None):
     kw = {}
     if size:
+        if which == "channel":
+            raise ValueError("the 128x64 channel has a fixed size")
         kw = dict(nx=size[0], ny=size[1])
-        if which == 3:
+        if which == "duct":
             if len(size) != 3:
-                raise ValueError("workload 3 takes --size nx ny nz")
+                raise ValueError("the duct takes --size nx ny nz")
             kw["nz"] = size[2]
         elif len(size) != 2:
             raise ValueError("2D workloads take --size nx ny")
-    if which == 1:
-        if size:
-            raise ValueError("workload 1 has a fixed size")
-        cfg, g, n = W.workload_config1(storage)
-    elif which == 2:
-        cfg, g, n = W.workload_config2(storage, **kw)
-    elif which == 3:
-        cfg, g, n = W.workload_config3(storage, **kw)
-    elif which == 4:
-        cfg, g, n = W.workload_config4(storage, **kw)
-    else:
-        raise ValueError("workload must be 1-4")
-    return cfg, g, n
+    if which == "channel":
+        return W.workload_channel_128x64(storage)
+    if which == "unsteady_channel":
+        return W.workload_unsteady_channel_1024x512(storage, **kw)
+    if which == "duct":
+        return W.workload_duct_256x128x128(storage, **kw)
+    if which == "thermal":
+        return W.workload_thermal_512x256(storage, **kw)
+    raise ValueError("unknown workload %r" % (which,))
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--workload", type=int, default=3)
+    ap.add_argument("--workload", choices=WORKLOADS, default="duct",
+                    help="channel: 128x64 D2Q9 BGK; unsteady_channel: 1024x512 D2Q9 BGK with "
+                         "pulsed inlet; duct: 256x128x128 D3Q19 MRT; thermal: 512x256 D2Q9 + D2Q5")
     ap.add_argument("--storage", choices=sorted(STORAGE), default="fp32")
     ap.add_argument("--size", type=int, nargs="+", default=None,
-                    help="nx ny nz (workload 3) or nx ny (workloads 2 and 4)")
+                    help="nx ny nz (duct) or nx ny (unsteady_channel, thermal)")
     ap.add_argument("--fwd", type=int, default=10)
     ap.add_argument("--adj", type=int, default=10)
     ap.add_argument("--autotune", action="store_true", help="pick block shapes first")

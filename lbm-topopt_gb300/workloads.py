@@ -136,13 +136,13 @@ def thermal_design(nx: int, ny: int, seed: int) -> np.ndarray:
 
 # -- the five workloads -------------------------------------------------------------
 
-def workload_config1(storage: int = STORE_FP64):
+def workload_channel_128x64(storage: int = STORE_FP64):
     """128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps from rest, pressure drop."""
     cfg = channel_2d(128, 64, storage=storage, nsteps=2000)
     return cfg, design_2d(128, 64, SEED_BASE + 1), 2000
 
 
-def workload_config2(storage: int = STORE_FP64, nx: int = 1024, ny: int = 512,
+def workload_unsteady_channel_1024x512(storage: int = STORE_FP64, nx: int = 1024, ny: int = 512,
                      nsteps: int = 20000):
     """1024x512 D2Q9 BGK + Brinkman, unsteady inlet, dissipated energy."""
     cfg = channel_2d(nx, ny, amp=0.2, period=2000.0, storage=storage,
@@ -150,14 +150,14 @@ def workload_config2(storage: int = STORE_FP64, nx: int = 1024, ny: int = 512,
     return cfg, design_2d(nx, ny, SEED_BASE + 2), nsteps
 
 
-def workload_config3(storage: int = STORE_FP64, nx: int = 256, ny: int = 128, nz: int = 128,
+def workload_duct_256x128x128(storage: int = STORE_FP64, nx: int = 256, ny: int = 128, nz: int = 128,
                      nsteps: int = 5000):
     """256x128x128 D3Q19 MRT + Brinkman duct, pressure drop."""
     cfg = duct_3d(nx, ny, nz, storage=storage, nsteps=nsteps)
     return cfg, design_3d(nx, ny, nz, SEED_BASE + 3), nsteps
 
 
-def workload_config4(storage: int = STORE_FP64, nx: int = 512, ny: int = 256,
+def workload_thermal_512x256(storage: int = STORE_FP64, nx: int = 512, ny: int = 256,
                      nsteps: int = 10000):
     """512x256 D2Q9 + D2Q5 thermal, oscillating inlet, heat flux out of the outlet."""
     cfg = thermal_2d(nx, ny, storage=storage, nsteps=nsteps)
@@ -167,7 +167,7 @@ def workload_config4(storage: int = STORE_FP64, nx: int = 512, ny: int = 256,
 BATCH_GRIDS = [(1024, 512)] * 3 + [(256, 128), (384, 192), (512, 256), (640, 320), (768, 384)]
 
 
-def workload_config5(storage: int = STORE_FP64, nsteps: int = 4000, scale: int = 1):
+def workload_batch_8_channels(storage: int = STORE_FP64, nsteps: int = 4000, scale: int = 1):
     """3 projected designs (beta=8, eta 0.3/0.5/0.7) of a 1024x512 channel plus 5 extra
     channels from independent seeds.  `scale` divides every grid edge (for tests)."""
     out = []

@@ -108,10 +108,10 @@ def test_seeded_workloads_are_reproducible():
     assert (a == b).all() and a.min() >= 0.0 and a.max() <= 1.0
     g = W.design_2d(128, 64, W.SEED_BASE + 1)
     assert g.shape == (128 * 64,) and 0.0 <= g.min() and g.max() <= 1.0
-    cfg, gamma, n = W.workload_config1()
+    cfg, gamma, n = W.workload_channel_128x64()
     assert (cfg.nx, cfg.ny, n) == (128, 64, 2000)
     assert abs(cfg.omega - 1.25) < 1e-15 and abs(cfg.interp_scale - 0.1) < 1e-15
-    insts, n5 = W.workload_config5(scale=8)
+    insts, n5 = W.workload_batch_8_channels(scale=8)
     assert len(insts) == 8 and n5 == 4000
     p = W.tanh_projection(np.linspace(0, 1, 11), 8.0, 0.5)
     assert abs(p[0]) < 1e-15 and abs(p[-1] - 1.0) < 1e-15

@@ -66,7 +66,7 @@ def test_batch_forward_matches_single(orc):
 def test_batch_d3q19_fp32_autotuned():
     cfgs, gs = [], []
     for k, (nx, ny, nz) in enumerate([(32, 16, 16), (24, 12, 12)]):
-        cfg, g, _ = W.workload_config3(G.STORE_FP32, nx=nx, ny=ny, nz=nz, nsteps=40)
+        cfg, g, _ = W.workload_duct_256x128x128(G.STORE_FP32, nx=nx, ny=ny, nz=nz, nsteps=40)
         cfgs.append(cfg)
         gs.append(g)
     with G.Batch(cfgs) as b:

@@ -25,7 +25,7 @@ N = 200
 
 @pytest.fixture(scope="module")
 def duct():
-    cfg, gamma, _ = W.workload_config3(G.STORE_FP32, nsteps=N)
+    cfg, gamma, _ = W.workload_duct_256x128x128(G.STORE_FP32, nsteps=N)
     return cfg, gamma
 
 

@@ -34,10 +34,10 @@ def run_gradient(cfg, gamma, n, k):
         return h.gradient(n, k)
 
 
-# -- configuration 1: 128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps --------------------
+# -- 128x64 channel: D2Q9 BGK + Brinkman, FP64, 2000 steps ---------------------------
 
-def test_config1_forward_matches_oracle(orc):
-    cfg, gamma, n = W.workload_config1()
+def test_channel_128x64_forward_matches_oracle(orc):
+    cfg, gamma, n = W.workload_channel_128x64()
     f, js, J, mac = run_forward(cfg, gamma, n)
     fo, jo, Jo = orc.forward(cfg, gamma, n)
     assert rel_inf(f, fo) < FP64_TOL
@@ -49,8 +49,8 @@ def test_config1_forward_matches_oracle(orc):
     assert rel_inf(m[:, 0], fr.sum(axis=1)) < FP64_TOL
 
 
-def test_config1_gradient_matches_oracle(orc):
-    cfg, gamma, _ = W.workload_config1()
+def test_channel_128x64_gradient_matches_oracle(orc):
+    cfg, gamma, _ = W.workload_channel_128x64()
     n = 400
     cfg = cfg.replace(obj_weight=1.0 / n)
     J, s, st = run_gradient(cfg, gamma, n, 16)
@@ -81,10 +81,10 @@ def test_mrt2d_forward_and_gradient(orc):
     assert rel_inf(s, so) < FP64_TOL
 
 
-# -- configuration 3 family: D3Q19 MRT + Brinkman duct --------------------------------
+# -- duct family: D3Q19 MRT + Brinkman ------------------------------------------------
 
 def test_d3q19_mrt_forward_matches_oracle(orc):
-    cfg, gamma, _ = W.workload_config3(nx=32, ny=16, nz=12, nsteps=150)
+    cfg, gamma, _ = W.workload_duct_256x128x128(nx=32, ny=16, nz=12, nsteps=150)
     f, js, J, mac = run_forward(cfg, gamma, 150)
     fo, jo, Jo = orc.forward(cfg, gamma, 150)
     assert rel_inf(f, fo) < FP64_TOL
@@ -92,7 +92,7 @@ def test_d3q19_mrt_forward_matches_oracle(orc):
 
 
 def test_d3q19_mrt_gradient_matches_oracle(orc):
-    cfg, gamma, _ = W.workload_config3(nx=20, ny=12, nz=10, nsteps=80)
+    cfg, gamma, _ = W.workload_duct_256x128x128(nx=20, ny=12, nz=10, nsteps=80)
     J, s, st = run_gradient(cfg, gamma, 80, 6)
     Jo, so = orc.gradient(cfg, gamma, 80)
     assert abs(J - Jo) <= FP64_TOL * abs(Jo)
@@ -100,7 +100,7 @@ def test_d3q19_mrt_gradient_matches_oracle(orc):
 
 
 def test_d3q19_bgk_forward_and_gradient(orc):
-    cfg, gamma, _ = W.workload_config3(nx=18, ny=10, nz=9, nsteps=60)
+    cfg, gamma, _ = W.workload_duct_256x128x128(nx=18, ny=10, nz=9, nsteps=60)
     cfg = cfg.replace(collision=G.BGK)
     f, _, _, _ = run_forward(cfg, gamma, 60)
     fo, _, _ = orc.forward(cfg, gamma, 60)
@@ -113,7 +113,7 @@ def test_d3q19_bgk_forward_and_gradient(orc):
 # -- thermal double distribution --------------------------------------------------------
 
 def test_thermal_forward_and_gradient(orc):
-    cfg, gamma, _ = W.workload_config4(nx=48, ny=24, nsteps=100)
+    cfg, gamma, _ = W.workload_thermal_512x256(nx=48, ny=24, nsteps=100)
     f, js, J, _ = run_forward(cfg, gamma, 100)
     fo, jo, Jo = orc.forward(cfg, gamma, 100)
     assert rel_inf(f, fo) < FP64_TOL
@@ -158,7 +158,7 @@ def test_adjoint_steps_match_oracle(orc):
 # -- reduced precision against the FP64 oracle -------------------------------------------
 
 def test_fp32_fp16_storage_error_vs_fp64_oracle(orc):
-    cfg, gamma, _ = W.workload_config3(nx=32, ny=16, nz=16, nsteps=200)
+    cfg, gamma, _ = W.workload_duct_256x128x128(nx=32, ny=16, nz=16, nsteps=200)
     fo, jo, Jo = orc.forward(cfg, gamma, 200)
     f32, _, J32, _ = run_forward(cfg.replace(storage=G.STORE_FP32), gamma, 200)
     f16, _, J16, _ = run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 200)
@@ -169,7 +169,7 @@ def test_fp32_fp16_storage_error_vs_fp64_oracle(orc):
 
 
 def test_fp32_gradient_vs_fp64_oracle(orc):
-    cfg, gamma, _ = W.workload_config3(nx=24, ny=12, nz=12, nsteps=120)
+    cfg, gamma, _ = W.workload_duct_256x128x128(nx=24, ny=12, nz=12, nsteps=120)
     Jo, so = orc.gradient(cfg, gamma, 120)
     J, s, _ = run_gradient(cfg.replace(storage=G.STORE_FP32), gamma, 120, 8)
     e = rel_l2(s, so)

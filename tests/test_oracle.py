@@ -133,7 +133,7 @@ def test_gradient_matches_central_differences(orc):
 
 
 def test_thermal_gradient_matches_central_differences(orc):
-    cfg, gamma, _ = W.workload_config4(nx=20, ny=10, nsteps=40)
+    cfg, gamma, _ = W.workload_thermal_512x256(nx=20, ny=10, nsteps=40)
     gamma = np.clip(gamma + 0.05 * np.sin(np.arange(gamma.size)), 0.02, 0.98)
     _, s = orc.gradient(cfg, gamma, 40)
     rng = np.random.default_rng(2)

@@ -81,7 +81,7 @@ def test_noalloc_objective_matches_forward(nlib, case, storage, tol):
         cfg = W.channel_2d(64, 32, amp=0.2, period=40.0, nsteps=60, storage=storage)
         gamma = W.design_2d(64, 32, 77)
     else:
-        cfg, gamma, _ = W.workload_config3(storage, nx=24, ny=12, nz=12, nsteps=60)
+        cfg, gamma, _ = W.workload_duct_256x128x128(storage, nx=24, ny=12, nz=12, nsteps=60)
     n = 60
     with G.Handle(cfg) as h:
         h.set_design(gamma)
@@ -97,7 +97,7 @@ def test_noalloc_objective_matches_forward(nlib, case, storage, tol):
 def test_noalloc_rejects_oversized_lattice(nlib):
     pytest.importorskip("torch")
     import torch
-    cfg, _, _ = W.workload_config3(G.STORE_FP32, nx=512, ny=256, nz=128, nsteps=10)
+    cfg, _, _ = W.workload_duct_256x128x128(G.STORE_FP32, nx=512, ny=256, nz=128, nsteps=10)
     dummy = torch.zeros(1, device="cuda")
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     c = cfg.to_c()
