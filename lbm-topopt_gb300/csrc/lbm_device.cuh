@@ -1210,28 +1210,6 @@ __device__ __forceinline__ void pair_halves(double e, double a, double& p, doubl
 }
 
 
-// d_i -= w_i (sum d + 3 e_i . sum e d): the increments then carry no mass and
-// no momentum (sum w = 1, sum w e = 0, sum w e e = I/3).
-template <int LAT, class C>
-__device__ __forceinline__ void project_conserved(C* d) {
-  using L = Lattice<LAT>;
-  C a = C(0.), bx = C(0.), by = C(0.), bz = C(0.);
-  static_for<L::QF>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    a += d[i];
-    if constexpr (L::ex(i) == 1) bx += d[i];
-    if constexpr (L::ex(i) == -1) bx -= d[i];
-    if constexpr (L::ey(i) == 1) by += d[i];
-    if constexpr (L::ey(i) == -1) by -= d[i];
-    if constexpr (L::ez(i) == 1) bz += d[i];
-    if constexpr (L::ez(i) == -1) bz -= d[i];
-  });
-  static_for<L::QF>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    d[i] -= C(L::w(i)) * (a + C(3.) * e_dot<LAT, i>(bx, by, bz));
-  });
-}
-
 // Increments of mrt3d_pair_collide (same operator: f + d is its output),
 // handed to emit(q, d_q) pair by pair so each pair's registers are freed early.
 template <class C, class Emit, class Emit2>
@@ -1265,42 +1243,98 @@ __device__ __forceinline__ void flow_collide_inc(const C* f, C imult, C& rho, C&
   using L = Lattice<LAT>;
   if constexpr (LAT == LAT_D3Q19 && COLL == LBM_MRT) {
     mrt3d_pair_collide_inc(f, imult, rho, jx, jy, jz, p, emit, emit2);
+  } else if constexpr (COLL == LBM_BGK) {
+    // BGK increments d_i = omega (feq_i - f_i), projected onto zero mass and
+    // momentum (d_i -= w_i (a + 3 e_i.b) with a = sum d, b = sum e d: then
+    // they carry none, as sum w = 1, sum w e = 0, sum w e e = I/3), then the
+    // partial bounce-back; all on the even and odd parts of each pair
+    // (k, k+H), ee = d_k + d_{k+H} and oo = d_k - d_{k+H}.  An even part
+    // carries its pair's mass and an odd part its momentum, so the
+    // projection subtracts 2 w_k a from ee and 6 w_k e_k.b from oo.
+    constexpr int H = L::HALF;
+    flow_macros<LAT>(f, rho, jx, jy, jz);
+    const C om = mp<C>(p).omega;
+    const C cFeq = rho - C(1.5) * (jx * jx + jy * jy + jz * jz);
+    C d0 = om * (C(L::w(0)) * cFeq - f[0]);
+    auto even = [&](auto K, C sc) -> C {
+      constexpr int k = decltype(K)::value;
+      return om * (C(2. * L::w(k)) * (cFeq + C(4.5) * sc * sc) - (f[k] + f[k + H]));
+    };
+    auto odd = [&](auto K, C sc) -> C {
+      constexpr int k = decltype(K)::value;
+      return om * (C(6. * L::w(k)) * sc - (f[k] - f[k + H]));
+    };
+    // D2Q9 keeps the parts in registers between the two passes; D3Q19
+    // recomputes them (same expressions, same values) to stay within its
+    // register budget
+    constexpr bool kKeep = H <= 4;
+    C ee[kKeep ? H : 1], oo[kKeep ? H : 1];
+    C a = d0, bx = C(0.), by = C(0.), bz = C(0.);
+    static_for<H>([&](auto D) {
+      constexpr int k = decltype(D)::value + 1;
+      const auto K = std::integral_constant<int, k>{};
+      const C sc = e_dot<LAT, k>(jx, jy, jz);
+      const C e = even(K, sc), o = odd(K, sc);
+      if constexpr (kKeep) {
+        ee[k - 1] = e;
+        oo[k - 1] = o;
+      }
+      a += e;
+      if constexpr (L::ex(k) == 1) bx += o;
+      if constexpr (L::ex(k) == -1) bx -= o;
+      if constexpr (L::ey(k) == 1) by += o;
+      if constexpr (L::ey(k) == -1) by -= o;
+      if constexpr (L::ez(k) == 1) bz += o;
+      if constexpr (L::ez(k) == -1) bz -= o;
+    });
+    emit(std::integral_constant<int, 0>{}, d0 - C(L::w(0)) * a);
+    const C twoim = C(2.) * imult;
+    static_for<H>([&](auto D) {
+      constexpr int k = decltype(D)::value + 1;
+      const auto K = std::integral_constant<int, k>{};
+      C e, o;
+      if constexpr (kKeep) {
+        e = ee[k - 1];
+        o = oo[k - 1];
+      } else {
+        const C sc = e_dot<LAT, k>(jx, jy, jz);
+        e = even(K, sc);
+        o = odd(K, sc);
+      }
+      const C E = e - C(2. * L::w(k)) * a;
+      const C O = o - C(6. * L::w(k)) * e_dot<LAT, k>(bx, by, bz);
+      // partial bounce-back moves imult ((f_{k+H} - f_k) + (d_{k+H} - d_k))
+      // from k+H to k: the odd part becomes O - 2 imult ((f_k - f_{k+H}) + O)
+      const C A = O - twoim * ((f[k] - f[k + H]) + O);
+      C dp, dm;
+      pair_halves(E, A, dp, dm);
+      emit2(std::integral_constant<int, k>{}, std::integral_constant<int, k + H>{}, dp, dm);
+    });
   } else {
+    // MRT on the 2D lattices: increments back-mapped from the relaxed
+    // non-conserved moments
     C d[L::QF];
     flow_macros<LAT>(f, rho, jx, jy, jz);
-    if constexpr (COLL == LBM_BGK) {
-      const C om = mp<C>(p).omega;
-      const C uSqr = jx * jx + jy * jy + jz * jz;
-      const C cFeq = rho - C(1.5) * uSqr;
-      static_for<L::QF>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        const C sc = e_dot<LAT, i>(jx, jy, jz);
-        const C eq = C(L::w(i)) * (cFeq + C(3.) * sc + C(4.5) * sc * sc);
-        d[i] = om * (eq - f[i]);
+    using M = MRT<L::DIM>;
+    C mo[M::K];
+    mrt_moments<L::DIM>(f, mo);
+    if (L::DIM == 2)
+      mrt2d_relax(mo, rho, jx, jy, p);
+    else
+      mrt3d_relax(mo, rho, jx, jy, jz, p);
+    static_for<M::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      C v = C(0.);
+      static_for<M::K>([&](auto KK) {
+        constexpr int k = decltype(KK)::value;
+        constexpr int c = M::m(k, i);
+        if constexpr (c != 0) {
+          constexpr double b = -(double)c / (double)M::n(k);
+          v += C(b) * mo[k];
+        }
       });
-      project_conserved<LAT>(d);
-    } else {
-      using M = MRT<L::DIM>;
-      C mo[M::K];
-      mrt_moments<L::DIM>(f, mo);
-      if (L::DIM == 2)
-        mrt2d_relax(mo, rho, jx, jy, p);
-      else
-        mrt3d_relax(mo, rho, jx, jy, jz, p);
-      static_for<M::QF>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        C v = C(0.);
-        static_for<M::K>([&](auto KK) {
-          constexpr int k = decltype(KK)::value;
-          constexpr int c = M::m(k, i);
-          if constexpr (c != 0) {
-            constexpr double b = -(double)c / (double)M::n(k);
-            v += C(b) * mo[k];
-          }
-        });
-        d[i] = v;
-      });
-    }
+      d[i] = v;
+    });
     emit(std::integral_constant<int, 0>{}, d[0]);
     // partial bounce-back on the collided values f + d, moving equal and
     // opposite amounts within each pair
@@ -1456,6 +1490,12 @@ __device__ __forceinline__ void eq_transpose_coeffs(const C* v, C jx, C jy, C jz
 
 // Increments d of flow_reverse<LAT, BGK> at input fin: lam + d is its output;
 // dg += dimult * d(out)/d(imult)^T lam.
+//
+// Evaluated on the sum and difference of each population pair (k, k+H): E^T v
+// has the even part c0 and the odd part e_k.c, and c0, c take the pair sums
+// v_k + v_{k+H} (weight w_k, and w_k e_k.u for the u-dependent part of c) and
+// differences v_k - v_{k+H} (weight w_k e_k).  The reverse partial bounce-back
+// keeps a pair's sum and scales its difference by 1 - 2 imult.
 template <int LAT, class C>
 __device__ __forceinline__ void bgk_reverse_inc(const C* fin, const C* lam, C* d, C imult,
                                                 C dimult, C& dg, const KParams& p) {
@@ -1464,48 +1504,72 @@ __device__ __forceinline__ void bgk_reverse_inc(const C* fin, const C* lam, C* d
   C rho, jx, jy, jz;
   flow_macros<LAT>(fin, rho, jx, jy, jz);
   const C om = mp<C>(p).omega;
-  const C cFeq = rho - C(1.5) * (jx * jx + jy * jy + jz * jz);
   // sensitivity to imult: sum over pairs of (fo_k - fo_opp)(lam_opp - lam_k),
-  // fo the collided state before partial bounce-back
+  // fo the collided state before partial bounce-back, whose pair difference
+  // is fd + omega (6 w_k e_k.j - fd) with fd = f_k - f_opp
   C imultRev = C(0.);
   static_for<H>([&](auto D) {
     constexpr int k = decltype(D)::value + 1;
-    const C sk = e_dot<LAT, k>(jx, jy, jz), so = e_dot<LAT, k + H>(jx, jy, jz);
-    const C fok = fin[k] + om * (C(L::w(k)) * (cFeq + C(3.) * sk + C(4.5) * sk * sk) - fin[k]);
-    const C foo = fin[k + H] + om * (C(L::w(k + H)) * (cFeq + C(3.) * so + C(4.5) * so * so) - fin[k + H]);
-    imultRev += (fok - foo) * (lam[k + H] - lam[k]);
+    const C fd = fin[k] - fin[k + H];
+    const C sc = e_dot<LAT, k>(jx, jy, jz);
+    imultRev += (fd + om * (C(6. * L::w(k)) * sc - fd)) * (lam[k + H] - lam[k]);
   });
   dg += dimult * imultRev;
-  // reverse partial bounce-back: mu = lam + m, m_k = imult (lam_opp - lam_k),
-  // recomputed where needed instead of held in registers
-  auto mpbb = [&](auto I) -> C {
-    constexpr int i = decltype(I)::value;
-    if constexpr (i == 0 || i > L::QF - 1) {
-      return C(0.);
-    } else if constexpr (i <= H) {
-      return imult * (lam[i + H] - lam[i]);
-    } else {
-      return -(imult * (lam[i] - lam[i - H]));
-    }
+  // c0 and c of E^T v from the rest value v0 and the pair sums vs(k) and
+  // differences vd(k)
+  auto transpose = [&](C v0, auto&& vs, auto&& vd, C& c0, C& cx, C& cy, C& cz) {
+    C p1x = C(0.), p1y = C(0.), p1z = C(0.), p2x = C(0.), p2y = C(0.), p2z = C(0.);
+    c0 = C(L::w(0)) * v0;
+    static_for<H>([&](auto D) {
+      constexpr int k = decltype(D)::value + 1;
+      const auto K = std::integral_constant<int, k>{};
+      const C ws = C(L::w(k)) * vs(K);
+      const C wd = C(L::w(k)) * vd(K);
+      const C sw = e_dot<LAT, k>(jx, jy, jz) * ws;
+      c0 += ws;
+      if constexpr (L::ex(k) == 1) { p1x += wd; p2x += sw; }
+      if constexpr (L::ex(k) == -1) { p1x -= wd; p2x -= sw; }
+      if constexpr (L::ey(k) == 1) { p1y += wd; p2y += sw; }
+      if constexpr (L::ey(k) == -1) { p1y -= wd; p2y -= sw; }
+      if constexpr (L::ez(k) == 1) { p1z += wd; p2z += sw; }
+      if constexpr (L::ez(k) == -1) { p1z -= wd; p2z -= sw; }
+    });
+    cx = C(3.) * (p1x - jx * c0) + C(9.) * p2x;
+    cy = C(3.) * (p1y - jy * c0) + C(9.) * p2y;
+    cz = C(3.) * (p1z - jz * c0) + C(9.) * p2z;
+  };
+  const C keep = C(1.) - C(2.) * imult;
+  auto lam_sum = [&](auto K) -> C {
+    constexpr int k = decltype(K)::value;
+    return lam[k] + lam[k + H];
+  };
+  auto mu_diff = [&](auto K) -> C {
+    constexpr int k = decltype(K)::value;
+    return keep * (lam[k] - lam[k + H]);
   };
   // reverse collision: omega (E^T mu - mu), projected with (I - E^T)
   C c0, cx, cy, cz;
-  {
-    C mu[L::QF];
-    static_for<L::QF>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      mu[i] = lam[i] + mpbb(I);
-    });
-    eq_transpose_coeffs<LAT>(mu, jx, jy, jz, c0, cx, cy, cz);
-    static_for<L::QF>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      d[i] = om * (c0 + e_dot<LAT, i>(cx, cy, cz) - mu[i]);
-    });
-  }
-  eq_transpose_coeffs<LAT>(d, jx, jy, jz, c0, cx, cy, cz);
-  static_for<L::QF>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    d[i] = (d[i] - (c0 + e_dot<LAT, i>(cx, cy, cz))) + mpbb(I);
+  transpose(lam[0], lam_sum, mu_diff, c0, cx, cy, cz);
+  const C d0 = om * (c0 - lam[0]);
+  C ds[H], dd[H];
+  static_for<H>([&](auto D) {
+    constexpr int k = decltype(D)::value + 1;
+    const auto K = std::integral_constant<int, k>{};
+    ds[k - 1] = om * (C(2.) * c0 - lam_sum(K));
+    dd[k - 1] = om * (C(2.) * e_dot<LAT, k>(cx, cy, cz) - mu_diff(K));
+  });
+  transpose(
+      d0, [&](auto K) -> C { return ds[decltype(K)::value - 1]; },
+      [&](auto K) -> C { return dd[decltype(K)::value - 1]; }, c0, cx, cy, cz);
+  d[0] = d0 - c0;
+  static_for<H>([&](auto D) {
+    constexpr int k = decltype(D)::value + 1;
+    // the reverse partial bounce-back adds imult (lam_opp - lam_k) to k and
+    // takes it from opp
+    const C es = ds[k - 1] - C(2.) * c0;
+    const C od = (dd[k - 1] - C(2.) * e_dot<LAT, k>(cx, cy, cz)) -
+                 C(2.) * imult * (lam[k] - lam[k + H]);
+    pair_halves(es, od, d[k], d[k + H]);
   });
 }
 
