@@ -178,6 +178,47 @@ def test_fp32_gradient_vs_fp64_oracle(orc):
     assert abs(J - Jo) < 1e-4 * abs(Jo)
 
 
+def _model(name):
+    if name == "d2q9_bgk":
+        cfg = W.channel_2d(48, 24, amp=0.2, period=100.0, nsteps=150)
+        return cfg, W.design_2d(48, 24, 11)
+    if name == "d2q9_mrt":
+        cfg = W.channel_2d(48, 24, collision=G.MRT, nsteps=150)
+        return cfg, W.design_2d(48, 24, 12)
+    if name == "d3q19_bgk":
+        cfg = W.duct_3d(20, 12, 10, nsteps=150).replace(collision=G.BGK)
+        return cfg, W.design_3d(20, 12, 10, 13)
+    cfg = W.thermal_2d(48, 24, nsteps=150)
+    return cfg, W.thermal_design(48, 24, 14)
+
+
+@pytest.mark.parametrize("name", ["d2q9_bgk", "d2q9_mrt", "d3q19_bgk", "thermal"])
+def test_reduced_precision_every_model_vs_fp64_oracle(orc, name):
+    """FP32 and FP16 storage of every other collision model against the FP64
+    oracle: populations after 150 steps (FP32 within 2e-6, FP16 within 2e-3
+    of the largest value) and the FP32 gradient (within 1e-4, rel. L2).  The
+    thermal lattice has no FP16 storage and says so."""
+    cfg, gamma = _model(name)
+    fo, _, _ = orc.forward(cfg, gamma, 150)
+    f32, _, _, _ = run_forward(cfg.replace(storage=G.STORE_FP32), gamma, 150)
+    if name == "thermal":
+        with pytest.raises(G.LBMError, match="FP64 or FP32 storage only"):
+            run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 150)
+        f16 = fo
+    else:
+        f16, _, _, _ = run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 150)
+    e32, e16 = rel_inf(f32, fo), rel_inf(f16, fo)
+    Jo, so = orc.gradient(cfg, gamma, 150)
+    J, s, _ = run_gradient(cfg.replace(storage=G.STORE_FP32), gamma, 150, 8)
+    eg = rel_l2(s, so)
+    print("%s: populations FP32 %.3e, FP16 %.3e; FP32 gradient %.3e, J %.3e"
+          % (name, e32, e16, eg, abs(J - Jo) / abs(Jo)))
+    assert e32 < 2e-6
+    assert e16 < 2e-3
+    assert eg < 1e-4
+    assert abs(J - Jo) < 1e-4 * abs(Jo)
+
+
 @pytest.mark.parametrize("lattice", ["d2q9", "d3q19", "thermal"])
 def test_fp32_fluid_cells_feel_no_porosity(lattice):
     """Where gamma = 1 the Brinkman term must vanish exactly in FP32 too: an
