@@ -1,6 +1,6 @@
 /*
  * design_oracle.c -- CPU restatement of the design-update chain of the
- * reference's optimisation loop (test infrastructure only: the checker the
+ * reference's optimisation loop (test infrastructure only: the oracle the
  * GPU design update is compared with).
  *
  *   density filter   topOpt/densityFilter2d.cc:33-146, densityFilter3d.cc:60-139

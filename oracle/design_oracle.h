@@ -1,5 +1,5 @@
 /* design_oracle.h -- CPU restatement of the design-update chain (density
- * filter, tanh projection, MMA) used only as the checker of the GPU design
+ * filter, tanh projection, MMA) used only as the oracle of the GPU design
  * update.  Test infrastructure. */
 #ifndef LBM_DESIGN_ORACLE_H
 #define LBM_DESIGN_ORACLE_H

@@ -2,7 +2,7 @@
  * lbm_oracle.c -- CPU restatement of the reference's forward/adjoint LBM hot
  * path, in plain C and FP64.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the pytest suite, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the pytest suite, the
  * package's smoke() and bench.py's CPU-baseline / reference arm call it to
  * produce the reference answer on the same inputs.  No product code path
  * links, loads or calls it.

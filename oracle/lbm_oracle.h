@@ -2,7 +2,7 @@
  * lbm_oracle.h -- CPU restatement of the reference LBM hot path (FP64).
  *
  * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline arm as the checker.  Never linked by the product.
+ * bench.py's CPU-baseline arm as the oracle.  Never linked by the product.
  *
  * All arrays are FP64 in DMDA order (cell c = (z*ny+y)*nx+x, AoS c*Q+q).
  * Return 0 on success, negative on error.

@@ -1,4 +1,4 @@
-"""ctypes access to the CPU checkers of the design update: the oracle's density
+"""ctypes access to the CPU oracles of the design update: the oracle's density
 filter, projection and MMA (oracle/design_oracle.c) and, where it was built,
 the reference's own MMA (topOpt/MMA.cc in oracle/_ref/libref.so).  Also the
 seeded MMA test problems the golden trajectories are made from.  Test

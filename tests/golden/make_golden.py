@@ -45,7 +45,7 @@ def cell_inputs(cfg, rng, n=16):
 def main():
     ref = reference()
     if ref is None:
-        raise SystemExit("build the reference checker first: make -C oracle ref")
+        raise SystemExit("build the reference operators first: make -C oracle ref")
     rng = np.random.default_rng(20261203)
     for name, (cfg, gamma, n) in cases().items():
         f, js, J = ref.forward(cfg, gamma, n)

@@ -1,4 +1,4 @@
-"""ctypes access to the CPU checkers: the C restatement (oracle/liblbmoracle.so)
+"""ctypes access to the CPU oracles: the C restatement (oracle/liblbmoracle.so)
 and, where it was built, the reference's own operators (oracle/_ref/libref.so).
 Test infrastructure only."""
 from __future__ import annotations
@@ -62,7 +62,7 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
-class Checker:
+class OracleLib:
     """Same calls for both libraries."""
 
     def __init__(self, path: str, prefix: str):
@@ -148,12 +148,12 @@ class Checker:
         return int(r.value), bool(ok.value), int(saved.value)
 
 
-def oracle() -> Checker:
-    return Checker(ORACLE_SO, "orc_")
+def oracle() -> OracleLib:
+    return OracleLib(ORACLE_SO, "orc_")
 
 
 def reference():
     """The reference build, or None where it was not built (no reference tree)."""
     if not os.path.exists(REF_SO):
         return None
-    return Checker(REF_SO, "ref_")
+    return OracleLib(REF_SO, "ref_")

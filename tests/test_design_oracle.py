@@ -1,4 +1,4 @@
-"""The design-update checker (oracle/design_oracle.c) on the CPU: its MMA
+"""The design-update oracle (oracle/design_oracle.c) on the CPU: its MMA
 against the reference's own MMA.cc (golden trajectories made by the reference
 build, and the reference build itself where present), and its density filter
 and projection against their defining properties (row normalisation, box and

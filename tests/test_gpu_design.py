@@ -1,4 +1,4 @@
-"""The design update on the GPU (lbm_topopt_*) against the CPU checker:
+"""The design update on the GPU (lbm_topopt_*) against the CPU oracle:
 
 * filter + projection chains (one and two stages, 2D and 3D, a filter box
   inside the grid) and their transposes within 1e-13 of the oracle;
