@@ -61,6 +61,7 @@ struct lbm_handle {
   Geometry geo_fwd;   // forward step (autotuned)
   Geometry geo_adj;   // reverse step (autotuned)
   bool adj_lean = false;   // reverse step: the register-lean variant (autotuned)
+  bool sens_atomic = false;   // reverse step adds to dJ/dgamma atomically (fits in L2)
   bool tuned = false;
   size_t partial_cap = 0;
   void* f[2] = {nullptr, nullptr};
@@ -159,6 +160,18 @@ void launch_max_change(size_t pop_bytes, const void* a, const void* b, int Q, lo
 
 size_t state_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->pop_bytes; }
 size_t adjoint_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->adj_bytes; }
+// Bytes one reverse step moves: the state, the adjoint in and out, the design
+// and the FP64 dJ/dgamma read and written.
+size_t reverse_step_bytes(const lbm_handle* h) {
+  return state_bytes(h) + 2 * adjoint_bytes(h) + (size_t)h->P * (h->gam_bytes + 16);
+}
+// Whether a reverse step of that many bytes stays in this device's L2.
+bool fits_in_l2(size_t bytes) {
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) return false;
+  return bytes <= (size_t)l2;
+}
 
 int check_box(const lbm_config& c, const int* b, int dim, const char* what) {
   int nz = dim == 3 ? c.nz : 1;
@@ -358,6 +371,7 @@ KParams base_params(const lbm_handle* h, int t) {
   p.accumulate = h->accumulate ? 1 : 0;
   p.gamma = h->gamma;
   p.sens = h->sens;
+  p.sens_atomic = h->sens_atomic ? 1 : 0;
   return p;
 }
 
@@ -543,6 +557,7 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   h->pop_bytes = c.storage == LBM_STORE_FP64 ? 8 : c.storage == LBM_STORE_FP32 ? 4 : 2;
   h->adj_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
   h->gam_bytes = c.storage == LBM_STORE_FP64 ? 8 : 4;
+  h->sens_atomic = fits_in_l2(reverse_step_bytes(h));
   h->launch = c.lattice == LBM_D2Q9    ? launcher_d2q9(c.collision, c.storage)
               : c.lattice == LBM_D3Q19 ? launcher_d3q19(c.collision, c.storage)
                                        : launcher_thermal(c.collision, c.storage);
@@ -1241,6 +1256,7 @@ struct lbm_batch {
   int bx = 128, by = 2;     // block shape of the forward and objective kernels
   int abx = 128, aby = 2;   // block shape of the reverse step kernel
   bool adj_lean = false;    // reverse step: the register-lean variant
+  bool sens_atomic = false; // the batched reverse step fits in L2 (see lbm_handle)
   int nsm = 1;
   int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
   cudaGraphExec_t graph = nullptr;
@@ -1396,6 +1412,7 @@ int batch_adjoint(lbm_batch* b, int buf) {
     p.lam_in = h->lam[h->lcur];
     p.lam_out = h->lam[1 - h->lcur];
     p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+    p.sens_atomic = b->sens_atomic ? 1 : 0;
   }
   int rc = batch_launch(b, b->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, bp, b->grid_adj);
   if (rc) return rc;
@@ -1574,6 +1591,9 @@ int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out) {
   b->by = b->aby = 2;
   batch_set_grids(b);
   b->grid_copy = 4 * b->nsm;
+  size_t rev = 0;
+  for (int i = 0; i < b->n; ++i) rev += reverse_step_bytes(b->h[i]);
+  b->sens_atomic = fits_in_l2(rev);
   *out = b;
   return LBM_OK;
 }

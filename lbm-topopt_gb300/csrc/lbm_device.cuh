@@ -239,6 +239,7 @@ struct KParams {
   const void* lam_in;      // eta_{t+1}
   void* lam_out;           // eta_t
   double* sens;
+  int sens_atomic;         // add to dJ/dgamma with an atomic (reverse steps that fit in L2)
 };
 
 template <class C>

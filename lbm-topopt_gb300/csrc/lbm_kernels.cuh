@@ -238,15 +238,17 @@ __device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, i
   return objv;
 }
 
-// dJ/dgamma(c) += dg.  D3Q19 adds with an atomic whose result is unused, so
-// the warp does not wait for the old value (reverse step 0.1605 to
-// 0.1558 ms on the 256x128x128 duct); the 2D lattices, whose reverse steps
-// carry more arithmetic per byte, keep the read-modify-write (the atomic
-// measured 2% slower there).  Either way one addition per cell and launch:
-// the same sum.
+// dJ/dgamma(c) += dg, one addition per cell and launch either way: the same
+// sum.  An atomic add whose result is unused lets the warp go on without
+// waiting for the old FP64 value; a read-modify-write keeps the addition on
+// the SM.  D3Q19 always takes the atomic (reverse step 0.1605 to 0.1558 ms on
+// the 256x128x128 duct).  The 2D lattices take it where the reverse step's
+// working set fits in L2 (p.sens_atomic, set by the host): on the 1024x512
+// channel it made the step 5% faster, while on a 4096x2048 lattice, streaming
+// from DRAM, it made it 2.5% slower.
 template <int LAT>
-__device__ __forceinline__ void add_sensitivity(double* sens, int c, double dg) {
-  if constexpr (LAT == LAT_D3Q19)
+__device__ __forceinline__ void add_sensitivity(double* sens, int c, double dg, int atomic) {
+  if (LAT == LAT_D3Q19 || atomic)
     atomicAdd(sens + c, dg);
   else
     sens[c] += dg;
@@ -318,7 +320,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
         lout[q * P + c] = Round<A>::apply(lam[q], d[q], rnd);
       });
     }
-    add_sensitivity<LAT>(p.sens, c, (double)dg);
+    add_sensitivity<LAT>(p.sens, c, (double)dg, p.sens_atomic);
     return;
   }
   if (LAT == LAT_D2Q9_D2Q5) {
@@ -339,7 +341,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
     constexpr int q = decltype(Q_)::value;
     lout[q * (int)p.P + c] = A(lam[q]);
   });
-  add_sensitivity<LAT>(p.sens, c, (double)dg);
+  add_sensitivity<LAT>(p.sens, c, (double)dg, p.sens_atomic);
 }
 
 // Objective of the state f_t at cell (x,y,z) alone.
