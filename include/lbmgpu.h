@@ -331,6 +331,11 @@ int lbm_batch_autotune(lbm_batch* b, int nsteps);
 int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by);
 /* Block shape of the batched reverse step kernel. */
 int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by);
+/* Set the block shape of the batched forward and objective kernels
+ * (which = 0) or of the batched reverse step (which = 1) to one of
+ * lbm_batch_autotune's shapes (256x1, 128x2, 64x4, 32x8, 128x1, 64x2, 32x4),
+ * e.g. one it found in an earlier run.  No reference counterpart. */
+int lbm_batch_set_launch_shape(lbm_batch* b, int which, int bx, int by);
 /* Register variant of the batched reverse step (as lbm_set_reverse_variant). */
 int lbm_batch_set_reverse_variant(lbm_batch* b, int lean);
 int lbm_batch_get_reverse_variant(const lbm_batch* b);

@@ -1727,6 +1727,25 @@ int lbm_batch_set_reverse_variant(lbm_batch* b, int lean) {
   return LBM_OK;
 }
 
+int lbm_batch_set_launch_shape(lbm_batch* b, int which, int bx, int by) {
+  if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
+  if (which < 0 || which > 1) return bfail(b, LBM_ERR_ARG, "which must be 0 (forward) or 1 (reverse)");
+  // the per-warp partial sums of every lattice are sized for the tuner's shapes
+  bool known = false;
+  for (const auto& sh : kShapes) known = known || (sh[0] == bx && sh[1] == by);
+  if (!known) return bfail(b, LBM_ERR_ARG, "block %dx%d is not one of the tuner's shapes", bx, by);
+  batch_destroy_graph(b);
+  if (which == 0) {
+    b->bx = bx;
+    b->by = by;
+  } else {
+    b->abx = bx;
+    b->aby = by;
+  }
+  batch_set_grids(b);
+  return LBM_OK;
+}
+
 int lbm_batch_get_reverse_variant(const lbm_batch* b) {
   if (!b) return bfail(nullptr, LBM_ERR_ARG, "null batch");
   return b->adj_lean ? 1 : 0;

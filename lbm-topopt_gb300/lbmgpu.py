@@ -204,6 +204,7 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_batch_autotune": (C.c_int, [H, C.c_int]),
         "lbm_batch_get_launch_shape": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "lbm_batch_get_reverse_shape": (C.c_int, [H, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_batch_set_launch_shape": (C.c_int, [H, C.c_int, C.c_int, C.c_int]),
         "lbm_batch_forward": (C.c_int, [H, C.c_int, dp]),
         "lbm_batch_gradient": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp, C.POINTER(dp),
                                          C.POINTER(CGradStats)]),
@@ -547,6 +548,11 @@ class Batch:
         bx, by = C.c_int(), C.c_int()
         self._check(self.lib.lbm_batch_get_reverse_shape(self.b, C.byref(bx), C.byref(by)))
         return bx.value, by.value
+
+    def set_launch_shape(self, which: int, bx: int, by: int):
+        """Block shape of the batched forward (which=0) or reverse (which=1)
+        step: one of the autotuner's shapes."""
+        self._check(self.lib.lbm_batch_set_launch_shape(self.b, int(which), int(bx), int(by)))
 
     def set_reverse_variant(self, lean: int):
         self._check(self.lib.lbm_batch_set_reverse_variant(self.b, int(lean)))

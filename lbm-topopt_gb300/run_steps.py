@@ -1,4 +1,4 @@
-"""Run forward and reverse time steps of one of the single-lattice workloads on the GPU.
+"""Run forward and reverse time steps of one of the workloads on the GPU.
 
     python lbm-topopt_gb300/run_steps.py --workload duct --storage fp32 --fwd 20 --adj 20
 
@@ -17,7 +17,7 @@ if HERE not in sys.path:
 import lbmgpu as G  # noqa: E402
 import workloads as W  # noqa: E402
 
-WORKLOADS = ("channel", "unsteady_channel", "duct", "thermal")
+WORKLOADS = ("channel", "unsteady_channel", "duct", "thermal", "batch")
 STORAGE = {"fp64": G.STORE_FP64, "fp32": G.STORE_FP32, "fp16": G.STORE_FP16}
 
 
@@ -44,11 +44,38 @@ def build_workload(which: str, storage: int, size=None):
     raise ValueError("unknown workload %r" % (which,))
 
 
+def run_batch(a):
+    """The 8-channel batch: one launch per step for all eight lattices."""
+    if a.size:
+        raise ValueError("the 8-channel batch has fixed sizes")
+    insts, _ = W.workload_batch_8_channels(STORAGE[a.storage])
+    n = sum(c.ncells for c, _ in insts)
+    with G.Batch([c for c, _ in insts]) as b:
+        for i, (_, g) in enumerate(insts):
+            b[i].set_design(g)
+            b[i].init_equilibrium()
+        if a.shape:
+            b.set_launch_shape(0, a.shape[0], a.shape[1])
+            b.set_launch_shape(1, a.shape[2], a.shape[3])
+        elif a.autotune:
+            print("block shapes (forward, reverse):", b.autotune(), b.reverse_shape())
+            for i, (_, g) in enumerate(insts):
+                b[i].init_equilibrium()
+        ms_f = b.time_steps(0, a.fwd) if a.fwd > 0 else 0.0
+        ms_a = b.time_steps(1, a.adj) if a.adj > 0 else 0.0
+        if a.fwd:
+            print("forward: %.4f ms/step, %.1f MLUPS" % (ms_f / a.fwd, n * a.fwd / ms_f / 1e3))
+        if a.adj:
+            print("adjoint: %.4f ms/step, %.1f MLUPS" % (ms_a / a.adj, n * a.adj / ms_a / 1e3))
+        print("kernel launches: %d" % b.launch_count())
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--workload", choices=WORKLOADS, default="duct",
                     help="channel: 128x64 D2Q9 BGK; unsteady_channel: 1024x512 D2Q9 BGK with "
-                         "pulsed inlet; duct: 256x128x128 D3Q19 MRT; thermal: 512x256 D2Q9 + D2Q5")
+                         "pulsed inlet; duct: 256x128x128 D3Q19 MRT; thermal: 512x256 D2Q9 + D2Q5; "
+                         "batch: 8 D2Q9 channels (3 of 1024x512, 256x128 .. 768x384)")
     ap.add_argument("--storage", choices=sorted(STORAGE), default="fp32")
     ap.add_argument("--size", type=int, nargs="+", default=None,
                     help="nx ny nz (duct) or nx ny (unsteady_channel, thermal)")
@@ -59,6 +86,8 @@ def main():
                     help="fixed block shapes of the forward and reverse steps (reproducible "
                          "profiles: the autotuner's choice can change under a profiler)")
     a = ap.parse_args()
+    if a.workload == "batch":
+        return run_batch(a)
     cfg, gamma, _ = build_workload(a.workload, STORAGE[a.storage], a.size)
     with G.Handle(cfg) as h:
         h.set_design(gamma)

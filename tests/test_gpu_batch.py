@@ -100,3 +100,28 @@ def test_batch_reverse_variant_does_not_change_results():
     assert np.allclose(out[0][0], out[1][0], rtol=1e-12, atol=0)
     for a, c in zip(out[0][1], out[1][1]):
         assert np.abs(a - c).max() <= 1e-7 * np.abs(a).max()
+
+
+def test_batch_launch_shape_does_not_change_results():
+    """Every shape the batch tuner may pick gives the same FP32 gradient bit
+    for bit (rounding streams are keyed by cell and step); shapes outside the
+    tuner's set are refused."""
+    n = 40
+    insts = uneven_2d(storage=G.STORE_FP32, n=n)
+    out = []
+    for fwd, rev in (((128, 2), (128, 2)), ((256, 1), (32, 4)), ((32, 8), (64, 2))):
+        with G.Batch([c for c, _ in insts]) as b:
+            for i, (_, g) in enumerate(insts):
+                b[i].set_design(g)
+            b.set_reverse_variant(0)
+            b.set_launch_shape(0, *fwd)
+            b.set_launch_shape(1, *rev)
+            assert b.reverse_shape() == rev
+            J, sens, _ = b.gradient(n, 7, use_graph=True)
+            out.append((J, sens))
+            with pytest.raises(G.LBMError, match="not one of the tuner's shapes"):
+                b.set_launch_shape(0, 96, 2)
+    for J, sens in out[1:]:
+        assert np.array_equal(J, out[0][0])
+        for a, c in zip(sens, out[0][1]):
+            assert np.array_equal(a, c)
