@@ -118,3 +118,34 @@ def test_seeded_workloads_are_reproducible():
 
 
 import numpy as np  # noqa: E402
+
+
+def handle_functions():
+    """Entry points whose first argument is a handle, batch or design-update
+    object."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(
+        r"^\s*(?:int|const char\*)\s+(lbm_\w+)\s*\(\s*(?:const\s+)?lbm_(?:handle|batch|topopt)\s*\*",
+        src, flags=re.M)))
+
+
+def test_null_handles_are_argument_errors(lib):
+    """Like a PETSc call on a null object: every entry point given a null
+    handle returns LBM_ERR_ARG (-1) with a message and touches nothing;
+    destroying a null handle is a no-op."""
+    names = handle_functions()
+    assert len(names) >= 50
+    for n in names:
+        f = getattr(lib, n)
+        assert f.argtypes is not None, n
+        args = [0.0 if t in (C.c_double, C.c_float) else
+                0 if t in (C.c_int, C.c_int64, C.c_uint, C.c_size_t) else None
+                for t in f.argtypes]
+        r = f(*args)
+        if n.endswith("_last_error"):
+            assert isinstance(r, bytes) and r, n
+        elif n.endswith("_destroy"):
+            assert r == 0, n
+        else:
+            assert r == -1, (n, r)
