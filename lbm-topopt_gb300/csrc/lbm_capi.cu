@@ -1330,7 +1330,9 @@ void batch_layout(lbm_batch* b, BatchParams& bp, int kind) {
     bp.start[i] = start;
     start += bp.gx[i] * bp.gy[i] * h->cfg.nz;
   }
-  bp.start[b->n] = start;
+  // slots past the batch start at the total (the kernels count the starts
+  // at or below a block)
+  for (int i = b->n; i <= kMaxBatch; ++i) bp.start[i] = start;
 }
 
 // Persistent grids of the batched kernels for the current block shapes.

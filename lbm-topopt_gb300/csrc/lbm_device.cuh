@@ -1991,7 +1991,7 @@ constexpr int kMaxBatch = LBM_MAX_BATCH;
 
 struct BatchParams {
   int n;                        // lattices in the batch
-  int start[kMaxBatch + 1];     // first virtual block of each lattice; start[n] = total
+  int start[kMaxBatch + 1];     // first virtual block of each lattice; start[n..kMaxBatch] = total
   int gx[kMaxBatch], gy[kMaxBatch];   // blocks along x and y of each lattice (z: one per plane)
   // ceil(2^32 / gx) and ceil(2^32 / gy) for batch_div, or 0 where the
   // multiply-high form does not apply (a divisor of 1, or a product n * d

@@ -407,13 +407,21 @@ __global__ void __launch_bounds__(256) k_objective(KParams p) {
 // with the resident blocks), so small and large lattices share the SMs.
 // Per-lattice parameters are read in place from the launch's parameter space.
 
+// Lattice of virtual block vb: the number of lattice starts at or below it
+// past the first.  The slots past the batch start at the total, and every
+// start is read at a fixed offset of the parameter space, with no loop.
+__device__ __forceinline__ int batch_lattice_of(const BatchParams& bp, int vb) {
+  int i = 0;
+  static_for<kMaxBatch - 1>([&](auto K) { i += vb >= bp.start[decltype(K)::value + 1] ? 1 : 0; });
+  return i;
+}
+
 template <int LAT, int COLL, class S>
 __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     k_forward_batch(const __grid_constant__ BatchParams bp) {
   step_prologue();
-  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
-    int i = 0;
-    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+  for (int vb = blockIdx.x; vb < bp.start[kMaxBatch]; vb += gridDim.x) {
+    const int i = batch_lattice_of(bp, vb);
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
     const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
@@ -430,9 +438,8 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
                                             : Occupancy<LAT, COLL, S>::adj)
     k_adjoint_batch(const __grid_constant__ BatchParams bp) {
   step_prologue();
-  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
-    int i = 0;
-    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+  for (int vb = blockIdx.x; vb < bp.start[kMaxBatch]; vb += gridDim.x) {
+    const int i = batch_lattice_of(bp, vb);
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
     const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
@@ -445,9 +452,8 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
 
 template <int LAT, class S>
 __global__ void __launch_bounds__(256) k_objective_batch(const __grid_constant__ BatchParams bp) {
-  for (int vb = blockIdx.x; vb < bp.start[bp.n]; vb += gridDim.x) {
-    int i = 0;
-    while (i + 1 < bp.n && vb >= bp.start[i + 1]) ++i;
+  for (int vb = blockIdx.x; vb < bp.start[kMaxBatch]; vb += gridDim.x) {
+    const int i = batch_lattice_of(bp, vb);
     const KParams& p = bp.p[i];
     const int lb = vb - bp.start[i];
     const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
