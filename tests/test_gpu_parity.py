@@ -308,6 +308,20 @@ def test_ragged_sizes(orc, nx, ny):
     assert rel_inf(s, so) < FP64_TOL
 
 
+def test_lattice_larger_than_l2_matches_oracle(orc):
+    """A 2D reverse step whose working set is larger than L2 adds to dJ/dgamma
+    with a read-modify-write (smaller ones use an atomic add): a 1536x768
+    channel, 283 MB per FP64 reverse step, against the oracle."""
+    nx, ny, n = 1536, 768, 8
+    assert nx * ny * (3 * 9 * 8 + 8 + 16) > 256 * 2**20
+    cfg = W.channel_2d(nx, ny, nsteps=n)
+    gamma = W.design_2d(nx, ny, 17)
+    J, s, _ = run_gradient(cfg, gamma, n, 3)
+    Jo, so = orc.gradient(cfg, gamma, n)
+    assert abs(J - Jo) <= FP64_TOL * abs(Jo)
+    assert rel_inf(s, so) < FP64_TOL
+
+
 def test_gradient_snapshot_counts_agree():
     cfg = W.channel_2d(24, 12, nsteps=50)
     gamma = W.design_2d(24, 12, 8)
