@@ -1300,9 +1300,10 @@ dim3 batch_block(const lbm_batch* b, int kind) {
 // one CTA per virtual block, as a single lattice's launch does, so that
 // programmatic dependent launch can schedule the next step's CTAs into the
 // previous step's last wave (a resident-CTA grid striding over the virtual
-// blocks cannot: the 8-channel D2Q9 batch took 43.2 / 64.9 us per forward
-// / reverse step that way, 38.8 / 62.0 us now).  The objective kernel keeps
-// a grid of resident CTAs striding over the blocks.
+// blocks cannot: measured on the 8-channel D2Q9 batch, 43.2 / 64.9 us per
+// forward / reverse step that way against 38.8 / 62.0 us with one CTA per
+// virtual block).  The objective kernel keeps a grid of resident CTAs
+// striding over the blocks.
 int batch_grid(lbm_batch* b, int kind, int total) {
   if (kind == K_FORWARD || kind == K_ADJOINT || kind == K_ADJOINT_LEAN) return total;
   int per_sm = 1;
