@@ -8,6 +8,7 @@ LaunchFn launcher_thermal(int collision, int storage) {
   if (collision == LBM_BGK) {
     if (storage == LBM_STORE_FP64) return &OpsImpl<LAT, LBM_BGK, double>::launch;
     if (storage == LBM_STORE_FP32) return &OpsImpl<LAT, LBM_BGK, float>::launch;
+    if (storage == LBM_STORE_FP16) return &OpsImpl<LAT, LBM_BGK, __half>::launch;
   }
   return nullptr;
 }
@@ -21,6 +22,10 @@ BatchOps batch_ops_thermal(int collision, int storage) {
   if (collision == LBM_BGK && storage == LBM_STORE_FP32) {
     o.launch = &OpsImpl<LAT, LBM_BGK, float>::launch_batch;
     o.kernel = &OpsImpl<LAT, LBM_BGK, float>::kernel_address;
+  }
+  if (collision == LBM_BGK && storage == LBM_STORE_FP16) {
+    o.launch = &OpsImpl<LAT, LBM_BGK, __half>::launch_batch;
+    o.kernel = &OpsImpl<LAT, LBM_BGK, __half>::kernel_address;
   }
   return o;
 }

@@ -189,9 +189,8 @@ int validate(const lbm_config& c) {
     return fail(nullptr, LBM_ERR_ARG, "unknown collision %d", c.collision);
   if (c.storage != LBM_STORE_FP64 && c.storage != LBM_STORE_FP32 && c.storage != LBM_STORE_FP16)
     return fail(nullptr, LBM_ERR_ARG, "unknown storage %d", c.storage);
-  if (c.lattice == LBM_D2Q9_D2Q5 && (c.collision != LBM_BGK || c.storage == LBM_STORE_FP16))
-    return fail(nullptr, LBM_ERR_SUP,
-                "the thermal lattice supports BGK flow with FP64 or FP32 storage only");
+  if (c.lattice == LBM_D2Q9_D2Q5 && c.collision != LBM_BGK)
+    return fail(nullptr, LBM_ERR_SUP, "the thermal lattice supports BGK flow only");
   int dim = c.lattice == LBM_D3Q19 ? 3 : 2;
   if (c.nx < 3 || c.ny < 3 || (dim == 3 && c.nz < 3))
     return fail(nullptr, LBM_ERR_ARG, "lattice %dx%dx%d too small (>= 3 cells per axis)", c.nx,

@@ -78,7 +78,7 @@ def test_bad_boundary_boxes_rejected(lib):
 
 def test_unsupported_combinations(lib):
     h = C.c_void_p()
-    cfg = W.thermal_2d(16, 8).replace(storage=G.STORE_FP16)
+    cfg = W.thermal_2d(16, 8).replace(collision=G.MRT)
     assert lib.lbm_create(C.byref(cfg.to_c()), C.byref(h)) == -2
     cfg = W.channel_2d(16, 8).replace(objective=G.OBJ_HEAT_FLUX)
     assert lib.lbm_create(C.byref(cfg.to_c()), C.byref(h)) == -2

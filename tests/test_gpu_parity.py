@@ -196,17 +196,11 @@ def _model(name):
 def test_reduced_precision_every_model_vs_fp64_oracle(orc, name):
     """FP32 and FP16 storage of every other collision model against the FP64
     oracle: populations after 150 steps (FP32 within 2e-6, FP16 within 2e-3
-    of the largest value) and the FP32 gradient (within 1e-4, rel. L2).  The
-    thermal lattice has no FP16 storage and says so."""
+    of the largest value) and the FP32 gradient (within 1e-4, rel. L2)."""
     cfg, gamma = _model(name)
     fo, _, _ = orc.forward(cfg, gamma, 150)
     f32, _, _, _ = run_forward(cfg.replace(storage=G.STORE_FP32), gamma, 150)
-    if name == "thermal":
-        with pytest.raises(G.LBMError, match="FP64 or FP32 storage only"):
-            run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 150)
-        f16 = fo
-    else:
-        f16, _, _, _ = run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 150)
+    f16, _, _, _ = run_forward(cfg.replace(storage=G.STORE_FP16), gamma, 150)
     e32, e16 = rel_inf(f32, fo), rel_inf(f16, fo)
     Jo, so = orc.gradient(cfg, gamma, 150)
     J, s, _ = run_gradient(cfg.replace(storage=G.STORE_FP32), gamma, 150, 8)
