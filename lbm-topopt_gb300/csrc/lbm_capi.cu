@@ -598,7 +598,15 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
     delete h;
     return fail(nullptr, LBM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
-  for (int i = 0; i < 4; ++i) cudaEventCreate(&h->ev[i]);
+  for (int i = 0; i < 4; ++i) {
+    e = cudaEventCreate(&h->ev[i]);
+    if (e != cudaSuccess) {
+      h->ev[i] = nullptr;
+      destroy_buffers(h);
+      delete h;
+      return fail(nullptr, LBM_ERR_CUDA, "cudaEventCreate: %s", cudaGetErrorString(e));
+    }
+  }
   ALLOC(h->f[0], state_bytes(h));
   ALLOC(h->f[1], state_bytes(h));
   ALLOC(h->lam[0], adjoint_bytes(h));
@@ -1586,8 +1594,13 @@ int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out) {
     delete b;
     return bfail(nullptr, LBM_ERR_CUDA, "batch set-up failed");
   }
-  cudaEventCreate(&b->ev[0]);
-  cudaEventCreate(&b->ev[1]);
+  for (cudaEvent_t& ev : b->ev) {
+    if (cudaEventCreate(&ev) != cudaSuccess) {
+      ev = nullptr;
+      lbm_batch_destroy(b);
+      return bfail(nullptr, LBM_ERR_CUDA, "batch set-up failed: cudaEventCreate");
+    }
+  }
   // default shapes: 128x2, one of the autotuner's shapes (partial sums are sized for all)
   b->bx = b->abx = 128;
   b->by = b->aby = 2;
