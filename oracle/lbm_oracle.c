@@ -1622,6 +1622,14 @@ int orc_time_steps(const lbm_config* cfg, const double* gamma, int nsteps, int n
     return -4;
   }
   init_equilibrium(&m, NULL, f);
+  /* first touch of every buffer outside the timed region, on the threads
+   * that use them (fresh pages would otherwise fault inside it) */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < S; ++i) {
+    tmp[i] = 0.;
+    lam[i] = 0.;
+  }
+  memset(sens, 0, sizeof(double) * m.ncell);
   double t0 = now_s();
   for (int t = 0; t < nsteps; ++t) {
     step(&m, f, tmp, gamma, t);

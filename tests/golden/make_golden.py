@@ -1,6 +1,6 @@
 """Generate the golden vectors in this directory from the reference's own
 operators, loops and checkpoint schedule (oracle/_ref/libref.so, built from the
-reference sources by `make -C oracle ref`).  The reference has no tests or
+reference sources by `make -C oracle ref REF_SRC=<reference>/src`).  The reference has no tests or
 stored results of its own; these fixtures are its outputs on seeded inputs.
 
     python tests/golden/make_golden.py
@@ -45,7 +45,7 @@ def cell_inputs(cfg, rng, n=16):
 def main():
     ref = reference()
     if ref is None:
-        raise SystemExit("build the reference operators first: make -C oracle ref")
+        raise SystemExit("build the reference operators first: make -C oracle ref REF_SRC=<reference>/src")
     rng = np.random.default_rng(20261203)
     for name, (cfg, gamma, n) in cases().items():
         f, js, J = ref.forward(cfg, gamma, n)

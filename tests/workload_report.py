@@ -1,6 +1,8 @@
-"""Measurements of the six workloads on the GPU, one JSON line each.
+"""Measurements of the six workloads on the GPU, one JSON line each, with the
+oracle as the checker (test infrastructure: it lives beside the tests because
+it imports the oracle; the product package does not).
 
-    python lbm-topopt_gb300/report.py [--workloads channel duct ...] [--quick]
+    python tests/workload_report.py [--workloads channel duct ...] [--quick]
 
 channel           128x64 D2Q9 BGK + Brinkman, FP64, 2000 steps: forward and
                   gradient time, agreement with the FP64 oracle.
@@ -33,6 +35,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "lbm-topopt_gb300"))
 sys.path.insert(0, HERE)
 
 import lbmgpu as G  # noqa: E402
@@ -40,7 +43,6 @@ import workloads as W  # noqa: E402
 
 
 def _oracle():
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import oracle
     return oracle()
 
@@ -203,7 +205,6 @@ def report_robust(quick):
     FP32 gradient, the chain rule of each realisation and one min-max MMA step
     with a fluid-volume constraint, all on the device; the CPU oracle's filter
     chain and MMA on the same inputs for comparison."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     import design_lib as D
     n = 400 if quick else 4000
     nx, ny = 1024, 512
