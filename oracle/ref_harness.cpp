@@ -12,12 +12,23 @@
  * ReverseIncompressibleBGK2d/MRT2d/MRT3d, ObstIsoCollisionLoop2d, IsoStreamLoop2d,
  * IsoEquilibriumInitializationLoop2d, SourceAdjointObstIsoCollisionLoop2d,
  * AdjointIsoStreamingLoop2d, the incompressible Zou-He boundary loops and their
- * adjoints, WangCheckpointing + DynamicCheckpointing.
+ * adjoints, WangCheckpointing + DynamicCheckpointing; for the thermal double
+ * distribution, ThermalDualCollision over PartialBouncebackCollision<BGK2d> and
+ * ThermalObstacleCollision<ThermalBGK2d<D2Q5>, RampInterpolation> with its
+ * getSourceAdjoint() operator (ReverseThermalDualCollision /
+ * ReverseThermalObstacleCollision / ReverseThermalBGK2d),
+ * SourceAdjointObstThermalCollisionLoop2d, ThermalFeq2d and
+ * AdjointThermalZouHeWest2d<D2Q9,D2Q5>.
  * Written out here because the reference does not compile them at HEAD: the 3D pull
  * stream and its transpose (a generalisation of isothermalLBLoops2d.hh:65-86 and
  * adjointIsothermalLBLoops2d.hh:139-163), the Hecht boundaries (Hecht3d.hh overrides a
  * two-argument execute) and their adjoints (adjointHecht3d.hh:35 does not parse), and
- * the functionals' evaluate/adjointCollideSource (they need the PETSc DMDA solver).
+ * the functionals' evaluate/adjointCollideSource (they need the PETSc DMDA solver); for
+ * the thermal lattice also the pull stream with mid-way bounce-back (the reference's
+ * thermal stream loops, dynamics/thermalStreamingLoop2d.hh:27-63, leave off-domain
+ * directions to explicit bounce-back boundaries), the forward ThermalZouHeWest2d
+ * (thermalZouHe2d.hh:68-80 overrides a two-argument execute) and
+ * ThermalOutflowEast2d (functionals/temperatureFlow2d.hh:18-54).
  */
 #include "petsc.h"
 
@@ -27,7 +38,12 @@
 #include "dynamics/incompressibleBGK2d.hh"
 #include "dynamics/incompressibleMRT2d.hh"
 #include "dynamics/partialBouncebackCollision.hh"
+#include "dynamics/thermalBGK2d.hh"
+#include "dynamics/thermalObstacleCollision.hh"
+#include "dynamics/thermalDualCollision.hh"
 #include "dynamics/isothermalLBLoops2d.hh"
+#include "adjointDynamics/adjointThermalLBLoops2d.hh"
+#include "adjointBoundaryConditions/adjointThermalZouHe2d.hh"
 #include "adjointDynamics/adjointIsothermalLBLoops2d.hh"
 #include "boundaryConditions/ZouHe2d.hh"
 #include "dynamics/equilibriumDistributions3d.hh"
@@ -148,7 +164,7 @@ template <class Base>
 struct Sim2d {
   using Op = PartialBouncebackCollision<Base, ScaledBP>;
   lbm_config c;
-  int nx, ny, Q = 9;
+  int nx, ny, Q = 9, NMAC = 3;
   Op op;
   Box2d box;
   std::vector<std::unique_ptr<LBBoundaryLoop>> bcs;
@@ -270,7 +286,7 @@ template <class C>
 struct Sim3d {
   using Op = PartialBouncebackCollision<MRT3dAdapter<C>, ScaledBP>;
   lbm_config c;
-  int nx, ny, nz, Q = 19;
+  int nx, ny, nz, Q = 19, NMAC = 4;
   Op op;
   Sim3d(const lbm_config& cfg)
       : c(cfg), nx(cfg.nx), ny(cfg.ny), nz(cfg.nz),
@@ -418,6 +434,146 @@ struct Sim3d {
   }
 };
 
+
+/* ------------------------------------------------------------------ */
+/* Thermal double distribution: D2Q9 BGK + partial bounce-back flow and D2Q5
+ * temperature, 14 DOF per cell (flow first, ThermalDualCollision's layout). */
+
+struct SimThermal {
+  using Iso = PartialBouncebackCollision<IncompressibleBGK2d<D2Q9>, ScaledBP>;
+  using Th = ThermalObstacleCollision<ThermalBGK2d<D2Q5>, RampInterpolation<>>;
+  using Op = ThermalDualCollision<Iso, Th>;
+  lbm_config c;
+  int nx, ny, Q = 14, NMAC = 4;
+  Op op;
+  Box2d box;
+  std::vector<std::unique_ptr<LBBoundaryLoop>> bcs;
+  std::vector<std::unique_ptr<AdjointLBBoundaryLoop>> abcs;
+
+  /* the thermal Zou-He inlets (restated: ThermalZouHeWest2d<.,D2Q5,.>::execute,
+   * thermalZouHe2d.hh:68-80) */
+  std::vector<lbm_bc> tbcs;
+
+  SimThermal(const lbm_config& cfg)
+      : c(cfg), nx(cfg.nx), ny(cfg.ny),
+        op(Iso(IncompressibleBGK2d<D2Q9>(cfg.omega), ScaledBP(cfg.interp_q, cfg.interp_scale)),
+           Th(ThermalBGK2d<D2Q5>(1., cfg.diffusivity), RampInterpolation<>(cfg.ramp_q, cfg.ramp_ck))),
+        box(0, cfg.nx - 1, 0, cfg.ny - 1) {
+    /* the reference has no solid heating term: only heat_rate = 0 is its model */
+    if (cfg.heat_rate != 0.) throw 3;
+    for (int k = 0; k < c.nbc; ++k) {
+      const lbm_bc& b = c.bc[k];
+      Box2d bb(b.box[0], b.box[1], b.box[2], b.box[3]);
+      LBBoundaryLoop* l = nullptr;
+      AdjointLBBoundaryLoop* al = nullptr;
+      if (b.kind == LBM_BC_VELOCITY) {
+        VelFunc vf{c, b};
+        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHeVelocityWest2d<D2Q9, VelFunc>(bb, vf);
+        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHeVelocityEast2d<D2Q9, VelFunc>(bb, vf);
+      } else if (b.kind == LBM_BC_PRESSURE) {
+        PresFunc pf{c, b};
+        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHePressureEast2d<D2Q9, PresFunc>(bb, pf);
+        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHePressureWest2d<D2Q9, PresFunc>(bb, pf);
+      } else if (b.kind == LBM_BC_TEMPERATURE && b.face == LBM_FACE_WEST) {
+        tbcs.push_back(b);
+        abcs.emplace_back(new AdjointThermalZouHeWest2d<D2Q9, D2Q5>(bb));
+        continue;
+      }
+      if (!l) throw 1;
+      bcs.emplace_back(l);
+      if (l->getAdjointBoundaryLoop(&al)) throw 2;
+      abcs.emplace_back(al);
+    }
+  }
+  size_t idx(int x, int y) const { return (size_t)y * nx + x; }
+
+  void init(const double* macros, std::vector<double>& f) {
+    for (size_t k = 0; k < (size_t)nx * ny; ++k) {
+      double rho = macros ? macros[4 * k] : 1., ux = macros ? macros[4 * k + 1] : 0.,
+             uy = macros ? macros[4 * k + 2] : 0., T = macros ? macros[4 * k + 3] : 0.;
+      IncompressibleFeq2d<D2Q9>::setAllEquilibria(&f[k * Q], rho, ux, uy, ux * ux + uy * uy);
+      ThermalFeq2d<D2Q5>::setAllEquilibria(&f[k * Q + 9], ux, uy, T);
+    }
+  }
+  void collide(std::vector<double>& f, std::vector<double>& mac, std::vector<double>& gamma) {
+    for (size_t k = 0; k < (size_t)nx * ny; ++k) op(&f[k * Q], &f[k * Q], &mac[4 * k], &gamma[k]);
+  }
+  template <class L>
+  void stream_lattice(std::vector<double>& f, const std::vector<double>& fl, int off) {
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x)
+        for (int d = 1; d < L::numDOF; ++d) {
+          int sx = x - L::ex[d], sy = y - L::ey[d];
+          if (sx >= 0 && sy >= 0 && sx < nx && sy < ny)
+            f[idx(x, y) * Q + off + d] = fl[idx(sx, sy) * Q + off + d];
+          else
+            f[idx(x, y) * Q + off + d] = fl[idx(x, y) * Q + off + L::opp[d]];
+        }
+  }
+  void stream(std::vector<double>& f, int t) {
+    std::vector<double> fl = f;
+    stream_lattice<D2Q9>(f, fl, 0);
+    stream_lattice<D2Q5>(f, fl, 9);
+    View2 vf(f.data(), nx, ny, Q);
+    for (auto& b : bcs) b->execute(t, vf.p, vf.p);
+    for (const lbm_bc& b : tbcs)
+      for (int y = b.box[2]; y <= b.box[3]; ++y) {
+        double* g = &f[idx(b.box[0], y) * Q + 9];
+        double T = b.value * time_factor(b, t);
+        g[4] = T - g[0] - g[1] - g[2] - g[3];
+      }
+  }
+  /* ThermalOutflowEast2d::evaluate (temperatureFlow2d.hh:18-32), summed without MPI */
+  double functional(const std::vector<double>& mac) {
+    if (c.objective != LBM_OBJ_HEAT_FLUX) return 0.;
+    double tc = c.obj_weight, pout = 0.;
+    for (int y = c.obj_out[2]; y <= c.obj_out[3]; ++y)
+      for (int x = c.obj_out[0]; x <= c.obj_out[1]; ++x)
+        pout -= tc * mac[idx(x, y) * 4 + 1] * mac[idx(x, y) * 4 + 3];
+    return pout;
+  }
+  /* ThermalOutflowEast2d::adjointCollideSource (temperatureFlow2d.hh:33-52) */
+  void source(std::vector<double>& adj, const std::vector<double>& f) {
+    if (c.objective != LBM_OBJ_HEAT_FLUX) return;
+    double tc = c.obj_weight;
+    for (int y = c.obj_out[2]; y <= c.obj_out[3]; ++y)
+      for (int x = c.obj_out[0]; x <= c.obj_out[1]; ++x) {
+        const double* fd = &f[idx(x, y) * Q];
+        double ux = 0., T;
+        IncompressibleMacros2d<D2Q9>::computeUx(fd, ux);
+        StandardThermalMacros2d<D2Q5>::compute(fd + 9, T);
+        double* a = &adj[idx(x, y) * Q];
+        for (int d = 0; d < 9; ++d) a[d] -= tc * D2Q9::ex[d] * T;
+        for (int d = 0; d < 5; ++d) a[9 + d] -= tc * ux;
+      }
+  }
+  template <class L>
+  void adjoint_stream_lattice(std::vector<double>& adj, const std::vector<double>& al, int off) {
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x)
+        for (int d = 1; d < L::numDOF; ++d) {
+          int sx = x + L::ex[d], sy = y + L::ey[d];
+          if (sx >= 0 && sy >= 0 && sx < nx && sy < ny)
+            adj[idx(x, y) * Q + off + d] = al[idx(sx, sy) * Q + off + d];
+          else
+            adj[idx(x, y) * Q + off + d] = al[idx(x, y) * Q + off + L::opp[d]];
+        }
+  }
+  void adjoint_step(std::vector<double>& adj, std::vector<double>& f, std::vector<double>& gamma,
+                    std::vector<double>& sens, int t) {
+    auto rop = op.getSourceAdjoint();
+    View2 va(adj.data(), nx, ny, Q), vf(f.data(), nx, ny, Q), vg(gamma.data(), nx, ny, 1);
+    Sens2 vs(sens.data(), nx, ny);
+    SourceAdjointObstThermalCollisionLoop2d<Op, decltype(rop)> aloop(box, rop);
+    aloop.execute(va.p, vf.p, vg.p, vs.p);
+    source(adj, f);
+    for (auto& b : abcs) b->execute(t, va.p, vf.p);
+    std::vector<double> al = adj;
+    adjoint_stream_lattice<D2Q9>(adj, al, 0);
+    adjoint_stream_lattice<D2Q5>(adj, al, 9);
+  }
+};
+
 /* ------------------------------------------------------------------ */
 /* Generic drivers (the reference applications' loop, robustPump2d.cc:234-276) */
 
@@ -425,8 +581,7 @@ template <class S>
 int run_forward(S& s, const lbm_config& c, const double* gamma, const double* macros, int n,
                 double* f_out, double* J_steps, double* J_sum) {
   size_t ncell = (size_t)c.nx * c.ny * (c.lattice == LBM_D3Q19 ? c.nz : 1);
-  int nmac = (c.lattice == LBM_D3Q19) ? 4 : 3;
-  std::vector<double> f(ncell * s.Q), mac(ncell * nmac), g(gamma, gamma + ncell);
+  std::vector<double> f(ncell * s.Q), mac(ncell * s.NMAC), g(gamma, gamma + ncell);
   s.init(macros, f);
   s.collide(f, mac, g);
   double acc = 0.;
@@ -447,8 +602,7 @@ template <class S>
 int run_gradient(S& s, const lbm_config& c, const double* gamma, const double* macros, int n,
                  double* J_sum, double* sens_out) {
   size_t ncell = (size_t)c.nx * c.ny * (c.lattice == LBM_D3Q19 ? c.nz : 1);
-  int nmac = (c.lattice == LBM_D3Q19) ? 4 : 3;
-  std::vector<double> f(ncell * s.Q), mac(ncell * nmac), g(gamma, gamma + ncell);
+  std::vector<double> f(ncell * s.Q), mac(ncell * s.NMAC), g(gamma, gamma + ncell);
   std::vector<std::vector<double>> states((size_t)n + 1);
   s.init(macros, f);
   states[0] = f;
@@ -495,6 +649,10 @@ int dispatch(const lbm_config& c, F&& fn) {
   }
   if (c.lattice == LBM_D3Q19 && c.collision == LBM_MRT && is_default3_rates(c)) {
     Sim3d<MRT3d_Compile_constants> s(c);
+    return fn(s);
+  }
+  if (c.lattice == LBM_D2Q9_D2Q5 && c.collision == LBM_BGK) {
+    SimThermal s(c);
     return fn(s);
   }
   return -2;
@@ -597,7 +755,7 @@ int ref_collide_cell(const lbm_config* cfg, const double* fin, double gamma, dou
       double g = gamma, m[4] = {0, 0, 0, 0};
       s.op(fin, fout, m, &g);
       if (mac)
-        for (int j = 0; j < (cfg->lattice == LBM_D3Q19 ? 4 : 3); ++j) mac[j] = m[j];
+        for (int j = 0; j < s.NMAC; ++j) mac[j] = m[j];
       return 0;
     });
   } catch (...) {

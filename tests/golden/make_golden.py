@@ -20,6 +20,15 @@ import workloads as W  # noqa: E402
 from oracle_lib import reference  # noqa: E402
 
 
+def thermal_case(nx, ny, nsteps):
+    """The thermal double distribution without the solid heating term (the
+    reference has none): a T = 1 Zou-He inlet heats the channel instead."""
+    cfg = W.thermal_2d(nx, ny, heat_rate=0.0, nsteps=nsteps, period=30.0)
+    bcs = [G.Boundary(b.kind, b.face, b.box, 1.0 if b.kind == G.BC_TEMPERATURE else b.value,
+                      b.profile, b.amp, b.period) for b in cfg.bcs]
+    return cfg.replace(bcs=bcs)
+
+
 def cases():
     return {
         "d2q9_bgk": (W.channel_2d(32, 16, amp=0.2, period=25.0, nsteps=120),
@@ -30,12 +39,15 @@ def cases():
         "d3q19_mrt": (W.duct_3d(16, 8, 8, nsteps=50), W.design_3d(16, 8, 8, 103), 50),
         "d3q19_mrt_default_rates": (W.duct_3d(12, 8, 8, nsteps=30).replace(mrt=G.MRT3D_DEFAULT),
                                     W.design_3d(12, 8, 8, 104), 30),
+        "d2q9_d2q5_thermal": (thermal_case(24, 12, 80), W.design_2d(24, 12, 106), 80),
     }
 
 
 def cell_inputs(cfg, rng, n=16):
-    base = {G.D2Q9: [4 / 9] + [1 / 36, 1 / 9] * 4,
-            G.D3Q19: [1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6}[cfg.lattice]
+    d2q9 = [4 / 9] + [1 / 36, 1 / 9] * 4
+    base = {G.D2Q9: d2q9,
+            G.D3Q19: [1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6,
+            G.D2Q9_D2Q5: d2q9 + [0.6 / 3] + [0.6 / 6] * 4}[cfg.lattice]
     fin = np.array(base)[None, :] * (1 + 0.05 * rng.standard_normal((n, len(base))))
     g = rng.uniform(0.02, 0.98, n)
     lo = rng.standard_normal((n, len(base)))
