@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define LBMGPU_ABI_VERSION 1
+#define LBMGPU_ABI_VERSION 2
 #define LBM_MAX_BC 8
 #define LBM_MAX_BATCH 8   /* lattices advanced by one batched launch */
 
@@ -61,22 +61,49 @@ extern "C" {
 #define LBM_STORE_FP32 1
 #define LBM_STORE_FP16 2
 
-/* Boundary condition kinds (applied after streaming on the boundary box). */
-#define LBM_BC_VELOCITY    1  /* Zou-He (2D, ZouHe2d.hh:23-56) / Hecht (3D, Hecht3d.hh:62-94) */
-#define LBM_BC_PRESSURE    2  /* Zou-He (ZouHe2d.hh:245-281) / Hecht (Hecht3d.hh:175-209) */
-#define LBM_BC_TEMPERATURE 3  /* thermal Zou-He Dirichlet (thermalZouHe2d.hh:63-97) */
+/* Boundary condition kinds (applied after streaming on the boundary box).
+ * Faces per kind, 2D (D2Q9 and the flow part of the thermal lattice):
+ *   LBM_BC_VELOCITY  west, east, north (IncompressibleZouHeVelocityWest/East/
+ *                    North2d, ZouHe2d.hh:23-133) and south (the mirror image of
+ *                    north; no reference counterpart)
+ *   LBM_BC_PRESSURE  west, east (IncompressibleZouHePressureWest/East2d,
+ *                    ZouHe2d.hh:241-321) and north, south (the east/west
+ *                    operator rotated onto the y faces; no reference counterpart)
+ *   LBM_BC_VELOCITY_STANDARD  west (StandardZouHeVelocityWest2d, ZouHe2d.hh:139-178):
+ *                    the standard-equilibrium density rho = (...)/(1 - ux)
+ *   LBM_BC_PRESSURE_STANDARD  west, east (StandardZouHePressureWest/East2d,
+ *                    ZouHe2d.hh:325-391)
+ *   LBM_BC_TEMPERATURE west (ThermalZouHeWest2d<.,D2Q5,.>, thermalZouHe2d.hh:63-97)
+ * 3D (D3Q19): LBM_BC_VELOCITY west (Hecht3d.hh:62-94), LBM_BC_PRESSURE east
+ * (Hecht3d.hh:175-209).  Other combinations return LBM_ERR_SUP, as the
+ * reference's boundary descriptors do (ZouHe2d.hh:181-236). */
+#define LBM_BC_VELOCITY          1
+#define LBM_BC_PRESSURE          2
+#define LBM_BC_TEMPERATURE       3
+#define LBM_BC_VELOCITY_STANDARD 4
+#define LBM_BC_PRESSURE_STANDARD 5
 
-/* Faces.  West = x min, East = x max, South = y min, North = y max,
- * Bottom = z min, Top = z max. */
+/* Faces.  West = x min, East = x max, South = y min, North = y max.  A
+ * boundary box lies on its face (x0 = x1 = 0 for west, y0 = y1 = ny-1 for
+ * north, ...) and may cover any segment of it. */
 #define LBM_FACE_WEST   0
 #define LBM_FACE_EAST   1
 #define LBM_FACE_SOUTH  2
 #define LBM_FACE_NORTH  3
 
-/* Inflow profiles.  value(t) = value * (1 + amp*sin(2*pi*t/period)). */
+/* Spatial profile of a boundary value over its box. */
 #define LBM_PROFILE_UNIFORM   0
-#define LBM_PROFILE_PARABOLIC 1  /* 2D: (m^2-(y-m)^2)/m^2, m=(ny-1)/2 (applications/diffuser/diffuser.cc:22-31);
-                                    3D: product of the y and z parabolas */
+#define LBM_PROFILE_PARABOLIC 1  /* across the lattice along the face: west/east faces
+                                    (m^2-(y-m)^2)/m^2, m=(ny-1)/2 (applications/diffuser/
+                                    diffuser.cc:22-31), times the same in z on D3Q19;
+                                    south/north faces the same across x, m=(nx-1)/2 */
+#define LBM_PROFILE_TABLE     2  /* tabulated by the caller with lbm_set_bc_profile */
+
+/* Time law of a boundary value: value(t) = value * T(t). */
+#define LBM_TIME_OFFSET_SINE 0  /* T(t) = 1 + amp*sin(2*pi*t/period) (amp = 0: steady) */
+#define LBM_TIME_SINE        1  /* T(t) = amp*sin(2*pi*t/period): zero mean, e.g. the
+                                   oscillating pump inlet of applications/RobustPump2d/
+                                   robustPump2d.cc:13-25 */
 
 /* Objectives (functionals/LBMacroFunctional.hh:6-14). */
 #define LBM_OBJ_NONE          0
@@ -84,15 +111,25 @@ extern "C" {
 #define LBM_OBJ_DISSIPATION   2  /* porous + viscous dissipated power (no reference counterpart) */
 #define LBM_OBJ_HEAT_FLUX     3  /* functionals/temperatureFlow2d.hh:10-63 */
 #define LBM_OBJ_OUTFLOW       4  /* -(mean u_x over obj_out): functionals/outflow2d.hh:10-54 */
+#define LBM_OBJ_THROUGH_FLOW  5  /* -(mean u_x over obj_in + mean u_x over obj_out):
+                                    functionals/throughFlow2d.hh:17-83 */
 
+/* One boundary condition: the reference's boundary loop plus its Input
+ * functor (ZouHe2d.hh:37: velocity or density as a function of the time step
+ * and the boundary cell).  At time step t and box cell i the prescribed value
+ * is v = value * T(t) * profile(i), and a velocity boundary imposes u = v * dir
+ * (dir = (0,0,0) means (1,0,0)); an LBM_PROFILE_TABLE boundary with a vector
+ * table takes u from the table instead. */
 typedef struct lbm_bc {
   int kind;        /* LBM_BC_* */
   int face;        /* LBM_FACE_* */
-  int profile;     /* LBM_PROFILE_* (velocity only) */
+  int profile;     /* LBM_PROFILE_* */
   int box[6];      /* x0,x1,y0,y1,z0,z1 inclusive; z0=z1=0 in 2D */
   double value;    /* u_max (velocity), rho0 (pressure), T (temperature) */
-  double amp;      /* relative oscillation amplitude, 0 = steady */
+  double amp;      /* relative oscillation amplitude of the time law */
   double period;   /* oscillation period in time steps */
+  int time_law;    /* LBM_TIME_* */
+  double dir[3];   /* velocity direction (velocity boundaries), (0,0,0) = +x */
 } lbm_bc;
 
 typedef struct lbm_config {
@@ -154,6 +191,25 @@ int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop);
 
 /* Lattice dimensions {nx, ny, nz} (nz = 1 in 2D). */
 int lbm_get_dims(const lbm_handle* h, int dims[3]);
+
+/* Tabulated input of boundary k, whose config gives it LBM_PROFILE_TABLE: the
+ * reference's Input functor (boundaryConditions/ZouHe2d.hh:37, e.g. the
+ * InflowVelocity of applications/RobustPump2d/robustPump2d.cc:13-25) sampled
+ * on the boundary cells for nt time steps, reused periodically (step t reads
+ * row t mod nt; nt = 1 for a profile that does not change in time).  A row
+ * holds npos = (cells of the box) entries, the box cells ordered along the
+ * face (y, then z, on west/east faces; x on south/north faces), each of ncomp
+ * values:
+ *   ncomp = 1       a factor: the cell's value is value * T(t) * entry and a
+ *                   velocity boundary imposes that times dir;
+ *   ncomp = 2 (2D) / 3 (D3Q19), velocity boundaries only: the velocity
+ *                   vector itself (value, time law and dir are not used).
+ * The table is copied to the device; calling again replaces it.  Steps that
+ * apply a table boundary whose table was never set return LBM_ERR_STATE.
+ * Set the tables of a batch's lattices before its first CUDA-graph gradient,
+ * or the captured graph keeps reading the old table.  No reference
+ * counterpart as an entry point (the reference takes a compiled functor). */
+int lbm_set_bc_profile(lbm_handle* h, int k, int nt, int ncomp, const double* table);
 
 /* Design field gamma in [0,1], one double per cell.  Replaces
  * LBSolver::setFieldFromDesignVec (latticeBoltzmann/LBSolver.cc:333-348). */

@@ -36,8 +36,40 @@ class IsothermalLBSolver {
     lbm_destroy(h_);
     h_ = nullptr;
     int rc = lbm_create(&cfg, &h_);
-    if (rc == LBM_OK) lbm_get_sizes(h_, &ncells_, &npop_);
+    if (rc == LBM_OK) {
+      lbm_get_sizes(h_, &ncells_, &npop_);
+      cfg_ = cfg;
+    }
     return rc;
+  }
+  // The reference's Input functor of a 2D Zou-He boundary (boundaryConditions/
+  // ZouHe2d.hh:37, e.g. InflowVelocity of applications/RobustPump2d/
+  // robustPump2d.cc:13-25) for boundary k, whose config has
+  // LBM_PROFILE_TABLE: the functor is sampled on the boundary's cells for
+  // `period` time steps, reused periodically (t mod period), and handed to
+  // lbm_set_bc_profile.  Velocity boundaries take
+  //   void operator()(long t, long i, long j, double& ux, double& uy) const;
+  template <class Input>
+  int setVelocityInput(int k, int period, const Input& in) {
+    std::vector<double> tab;
+    int npos = sample(k, period, 2, &tab, [&](long t, long i, long j, double* v) {
+      in(t, i, j, v[0], v[1]);
+    });
+    if (npos < 0) return LBM_ERR_ARG;
+    return lbm_set_bc_profile(h_, k, period, 2, tab.data());
+  }
+  // Pressure and temperature boundaries take
+  //   void operator()(long t, long i, long j, double& value) const;
+  // whose value multiplies the boundary's value * T(t) (a config value of 1
+  // with no oscillation takes the functor's value as it is).
+  template <class Input>
+  int setScalarInput(int k, int period, const Input& in) {
+    std::vector<double> tab;
+    int npos = sample(k, period, 1, &tab, [&](long t, long i, long j, double* v) {
+      in(t, i, j, v[0]);
+    });
+    if (npos < 0) return LBM_ERR_ARG;
+    return lbm_set_bc_profile(h_, k, period, 1, tab.data());
   }
   // LBSolver::setFieldFromDesignVec (LBSolver.cc:333-348)
   int setFieldFromDesignVec(const std::vector<double>& gamma) {
@@ -74,7 +106,26 @@ class IsothermalLBSolver {
   int numPopulations() const { return npop_; }
 
  private:
+  // values of boundary k's cells (along the face: y on west/east faces, x on
+  // south/north faces) for t = 0..period-1; -1 for a bad boundary or period
+  template <class F>
+  int sample(int k, int period, int ncomp, std::vector<double>* tab, F f) const {
+    if (!h_ || k < 0 || k >= cfg_.nbc || period < 1) return -1;
+    const lbm_bc& b = cfg_.bc[k];
+    const bool yface = b.face == LBM_FACE_SOUTH || b.face == LBM_FACE_NORTH;
+    const int s0 = yface ? b.box[0] : b.box[2], s1 = yface ? b.box[1] : b.box[3];
+    const int npos = s1 - s0 + 1;
+    tab->assign((size_t)period * npos * ncomp, 0.);
+    for (int t = 0; t < period; ++t)
+      for (int s = s0; s <= s1; ++s) {
+        const long i = yface ? s : b.box[0], j = yface ? b.box[2] : s;
+        f(t, i, j, tab->data() + ((size_t)t * npos + (s - s0)) * ncomp);
+      }
+    return npos;
+  }
+
   lbm_handle* h_ = nullptr;
+  lbm_config cfg_{};
   int64_t ncells_ = 0;
   int npop_ = 0;
 };

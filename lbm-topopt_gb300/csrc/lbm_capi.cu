@@ -23,6 +23,91 @@
 
 using namespace lbm;
 
+namespace lbm {
+
+bool bc_on_y_face(const lbm_bc& b) { return b.face == LBM_FACE_SOUTH || b.face == LBM_FACE_NORTH; }
+
+int64_t bc_npos(const lbm_bc& b) {
+  if (bc_on_y_face(b)) return (int64_t)(b.box[1] - b.box[0] + 1) * (b.box[5] - b.box[4] + 1);
+  return (int64_t)(b.box[3] - b.box[2] + 1) * (b.box[5] - b.box[4] + 1);
+}
+
+double bc_time_factor(const lbm_bc& b, int t) {
+  if (b.time_law == LBM_TIME_SINE)
+    return b.amp == 0. ? 0. : b.amp * sin(2. * M_PI * (double)t / b.period);
+  return (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
+}
+
+// (m^2 - (s-m)^2)/m^2 across the lattice along the face (m = (n-1)/2 of the
+// tangential axis; applications/diffuser/diffuser.cc:22-31), times the same
+// in z on D3Q19.
+void bc_parabola(const lbm_config& c, const lbm_bc& b, double* out) {
+  const bool yface = bc_on_y_face(b);
+  const int n = yface ? c.nx : c.ny;
+  const int s0 = yface ? b.box[0] : b.box[2], s1 = yface ? b.box[1] : b.box[3];
+  const int ns = s1 - s0 + 1;
+  for (int z = b.box[4]; z <= b.box[5]; ++z)
+    for (int s = s0; s <= s1; ++s) {
+      double mid = (double)(n - 1) / 2.;
+      double pr = (mid * mid - (s - mid) * (s - mid)) / (mid * mid);
+      if (c.lattice == LBM_D3Q19) {
+        double mz = (double)(c.nz - 1) / 2.;
+        pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
+      }
+      out[(size_t)(z - b.box[4]) * ns + (s - s0)] = pr;
+    }
+}
+
+void fill_devbc(const lbm_bc& b, int t, int ncomp, const double* tab_d, const float* tab_f,
+                DevBC& d) {
+  d.kind = b.kind;
+  d.face = b.face;
+  d.profile = b.profile;
+  for (int i = 0; i < 6; ++i) d.box[i] = b.box[i];
+  d.tang_x = bc_on_y_face(b) ? 1 : 0;
+  d.n_t = d.tang_x ? b.box[1] - b.box[0] + 1 : b.box[3] - b.box[2] + 1;
+  d.ncomp = tab_d ? ncomp : 0;
+  // value(t) = value * T(t), evaluated here once per launch
+  d.value = b.value * bc_time_factor(b, t);
+  d.value_f = (float)d.value;
+  d.vshift = d.value - 1.;
+  d.vshift_f = (float)d.vshift;
+  const bool nodir = b.dir[0] == 0. && b.dir[1] == 0. && b.dir[2] == 0.;
+  for (int a = 0; a < 3; ++a) {
+    d.dir[a] = nodir ? (a == 0 ? 1. : 0.) : b.dir[a];
+    d.dir_f[a] = (float)d.dir[a];
+  }
+  d.prof = tab_d;
+  d.prof_f = tab_f;
+}
+
+bool objective_info(int id, ObjectiveInfo* out) {
+  for (int k = 0; k < objective_count(ObjectiveList{}); ++k) {
+    const ObjectiveInfo oi = objective_info_at(ObjectiveList{}, k);
+    if (oi.id == id) {
+      if (out) *out = oi;
+      return true;
+    }
+  }
+  return false;
+}
+
+void objective_norms(const lbm_config& c, double* inv_in, double* inv_out) {
+  *inv_in = *inv_out = 0.;
+  ObjectiveInfo oi;
+  if (c.objective == LBM_OBJ_NONE || !objective_info(c.objective, &oi)) return;
+  if (oi.uses & kUsesIn) {
+    const int* a = c.obj_in;
+    *inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
+  }
+  if (oi.uses & kUsesOut) {
+    const int* b = c.obj_out;
+    *inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
+  }
+}
+
+}  // namespace lbm
+
 namespace {
 
 thread_local std::string g_create_error;
@@ -77,8 +162,13 @@ struct lbm_handle {
   double* stage = nullptr;     // FP64 AoS staging (ncell*Q)
   double* init_mac = nullptr;  // initial macros kept for lbm_gradient (device, may be null)
   std::vector<void*> slots;
-  double* bcprof_d[LBM_MAX_BC] = {};   // inflow profile per boundary (device)
+  // per boundary: parabolic factors or the caller's table (lbm_set_bc_profile),
+  // tab_nt rows of bc_npos * tab_ncomp values (device, FP64 and FP32 copies)
+  double* bcprof_d[LBM_MAX_BC] = {};
   float* bcprof_f[LBM_MAX_BC] = {};
+  int tab_nt[LBM_MAX_BC] = {};
+  int tab_ncomp[LBM_MAX_BC] = {};
+  int64_t table_gen = 0;   // bumped when a table moves to a new device buffer
   int t = 0;
   bool have_design = false, have_state = false, have_adjoint = false;
   bool accumulate = false;   // objective sums over steps into the warp partials
@@ -209,41 +299,75 @@ int validate(const lbm_config& c) {
     const lbm_bc& b = c.bc[k];
     int rc = check_box(c, b.box, dim, "boundary");
     if (rc) return rc;
-    bool ok = false;
-    if (b.kind == LBM_BC_VELOCITY || b.kind == LBM_BC_PRESSURE) {
-      if (b.face == LBM_FACE_WEST) ok = (b.box[0] == 0 && b.box[1] == 0);
-      if (b.face == LBM_FACE_EAST) ok = (b.box[0] == c.nx - 1 && b.box[1] == c.nx - 1);
-      if (dim == 3 && !((b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) ||
-                        (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_EAST)))
+    if (b.face < LBM_FACE_WEST || b.face > LBM_FACE_NORTH)
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: unknown face %d", k, b.face);
+    // the operators each kind has per face (the reference's descriptors give
+    // PETSC_ERR_SUP for the others, boundaryConditions/ZouHe2d.hh:181-236)
+    const int w = 1 << LBM_FACE_WEST, e = 1 << LBM_FACE_EAST, all = 15;
+    int faces = 0;
+    if (dim == 3) {
+      faces = b.kind == LBM_BC_VELOCITY ? w : b.kind == LBM_BC_PRESSURE ? e : 0;
+      if (!((1 << b.face) & faces))
         return fail(nullptr, LBM_ERR_SUP,
                     "D3Q19 supports the Hecht velocity west and pressure east faces only");
-    } else if (b.kind == LBM_BC_TEMPERATURE) {
-      if (c.lattice != LBM_D2Q9_D2Q5)
-        return fail(nullptr, LBM_ERR_SUP, "temperature boundary needs the thermal lattice");
-      ok = (b.face == LBM_FACE_WEST && b.box[0] == 0 && b.box[1] == 0);
     } else {
-      return fail(nullptr, LBM_ERR_SUP, "boundary kind %d not supported", b.kind);
+      switch (b.kind) {
+        case LBM_BC_VELOCITY:
+        case LBM_BC_PRESSURE:
+          faces = all;
+          break;
+        case LBM_BC_VELOCITY_STANDARD:
+          faces = w;
+          break;
+        case LBM_BC_PRESSURE_STANDARD:
+          faces = w | e;
+          break;
+        case LBM_BC_TEMPERATURE:
+          if (c.lattice != LBM_D2Q9_D2Q5)
+            return fail(nullptr, LBM_ERR_SUP, "temperature boundary needs the thermal lattice");
+          faces = w;
+          break;
+        default:
+          return fail(nullptr, LBM_ERR_SUP, "boundary kind %d not supported", b.kind);
+      }
+      if (!((1 << b.face) & faces))
+        return fail(nullptr, LBM_ERR_SUP, "boundary %d: kind %d has no operator on face %d", k,
+                    b.kind, b.face);
+    }
+    bool ok = false;
+    switch (b.face) {
+      case LBM_FACE_WEST: ok = b.box[0] == 0 && b.box[1] == 0; break;
+      case LBM_FACE_EAST: ok = b.box[0] == c.nx - 1 && b.box[1] == c.nx - 1; break;
+      case LBM_FACE_SOUTH: ok = b.box[2] == 0 && b.box[3] == 0; break;
+      default: ok = b.box[2] == c.ny - 1 && b.box[3] == c.ny - 1; break;
     }
     if (!ok) return fail(nullptr, LBM_ERR_ARG, "boundary %d: box does not lie on its face", k);
+    if (b.profile != LBM_PROFILE_UNIFORM && b.profile != LBM_PROFILE_PARABOLIC &&
+        b.profile != LBM_PROFILE_TABLE)
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: unknown profile %d", k, b.profile);
+    if (b.time_law != LBM_TIME_OFFSET_SINE && b.time_law != LBM_TIME_SINE)
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: unknown time law %d", k, b.time_law);
     if (b.amp != 0. && !(b.period > 0.))
       return fail(nullptr, LBM_ERR_ARG, "boundary %d: oscillation needs period > 0", k);
-    if (!std::isfinite(b.value)) return fail(nullptr, LBM_ERR_ARG, "boundary %d: bad value", k);
+    if (!std::isfinite(b.value) || !std::isfinite(b.amp))
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: bad value", k);
+    for (int a = 0; a < 3; ++a)
+      if (!std::isfinite(b.dir[a])) return fail(nullptr, LBM_ERR_ARG, "boundary %d: bad direction", k);
   }
-  if (c.objective == LBM_OBJ_PRESSURE_DROP) {
-    int rc = check_box(c, c.obj_in, dim, "objective inflow");
-    if (rc) return rc;
-    rc = check_box(c, c.obj_out, dim, "objective outflow");
-    if (rc) return rc;
-  } else if (c.objective == LBM_OBJ_HEAT_FLUX) {
-    if (c.lattice != LBM_D2Q9_D2Q5)
-      return fail(nullptr, LBM_ERR_SUP, "heat flux objective needs the thermal lattice");
-    int rc = check_box(c, c.obj_out, dim, "objective outflow");
-    if (rc) return rc;
-  } else if (c.objective == LBM_OBJ_OUTFLOW) {
-    int rc = check_box(c, c.obj_out, dim, "objective outflow");
-    if (rc) return rc;
-  } else if (c.objective != LBM_OBJ_NONE && c.objective != LBM_OBJ_DISSIPATION) {
-    return fail(nullptr, LBM_ERR_ARG, "unknown objective %d", c.objective);
+  if (c.objective != LBM_OBJ_NONE) {
+    ObjectiveInfo oi;
+    if (!objective_info(c.objective, &oi))
+      return fail(nullptr, LBM_ERR_ARG, "unknown objective %d", c.objective);
+    if (oi.thermal && c.lattice != LBM_D2Q9_D2Q5)
+      return fail(nullptr, LBM_ERR_SUP, "objective %d needs the thermal lattice", c.objective);
+    if (oi.uses & kUsesIn) {
+      int rc = check_box(c, c.obj_in, dim, "objective inflow");
+      if (rc) return rc;
+    }
+    if (oi.uses & kUsesOut) {
+      int rc = check_box(c, c.obj_out, dim, "objective outflow");
+      if (rc) return rc;
+    }
   }
   return 0;
 }
@@ -305,20 +429,14 @@ KParams base_params(const lbm_handle* h, int t) {
   p.apply_bc = t >= 1;
   for (int k = 0; k < c.nbc; ++k) {
     const lbm_bc& b = c.bc[k];
-    DevBC& d = p.bc[k];
-    d.kind = b.kind;
-    d.face = b.face;
-    d.profile = b.profile;
-    for (int i = 0; i < 6; ++i) d.box[i] = b.box[i];
-    // value(t) = value * (1 + amp sin(2 pi t / period)), evaluated here once per launch
-    double tf = (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
-    d.value = b.value * tf;
-    d.value_f = (float)d.value;
-    d.vshift = d.value - 1.;
-    d.vshift_f = (float)d.vshift;
-    d.prof = h->bcprof_d[k];
-    d.prof_f = h->bcprof_f[k];
-    d.ny_box = b.box[3] - b.box[2] + 1;
+    // a table row per time step (t mod nt); parabolic factors have one row
+    const int64_t row = h->tab_nt[k] > 0 ? (int64_t)(t % h->tab_nt[k]) * bc_npos(b) *
+                                               (h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1)
+                                         : 0;
+    fill_devbc(b, t, h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1,
+               h->bcprof_d[k] ? h->bcprof_d[k] + row : nullptr,
+               h->bcprof_f[k] ? h->bcprof_f[k] + row : nullptr, p.bc[k]);
+    if (bc_on_y_face(b)) p.bc_y = 1;
   }
   p.objective = c.objective;
   p.obj_weight = c.obj_weight;
@@ -326,14 +444,7 @@ KParams base_params(const lbm_handle* h, int t) {
     p.obj_in[i] = c.obj_in[i];
     p.obj_out[i] = c.obj_out[i];
   }
-  if (c.objective == LBM_OBJ_PRESSURE_DROP) {
-    const int* a = c.obj_in;
-    p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
-  }
-  if (c.objective == LBM_OBJ_PRESSURE_DROP || c.objective == LBM_OBJ_OUTFLOW) {
-    const int* b = c.obj_out;
-    p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
-  }
+  objective_norms(c, &p.inv_in, &p.inv_out);
   ModelParams<double>& md = p.md;
   md.omega = c.omega;
   for (int i = 0; i < 8; ++i) md.mrt[i] = c.mrt[i];
@@ -374,7 +485,21 @@ KParams base_params(const lbm_handle* h, int t) {
   return p;
 }
 
+// A boundary with LBM_PROFILE_TABLE whose table lbm_set_bc_profile never set
+// (-1 if none).
+int missing_table(const lbm_handle* h) {
+  for (int k = 0; k < h->cfg.nbc; ++k)
+    if (h->cfg.bc[k].profile == LBM_PROFILE_TABLE && !h->bcprof_d[k]) return k;
+  return -1;
+}
+
 int launch(lbm_handle* h, int kind, const KParams& p, double* aux) {
+  if (p.apply_bc) {
+    const int k = missing_table(h);
+    if (k >= 0)
+      return fail(h, LBM_ERR_STATE, "boundary %d has LBM_PROFILE_TABLE but no table "
+                  "(lbm_set_bc_profile)", k);
+  }
   const Geometry& g = kind == K_FORWARD                              ? h->geo_fwd
                       : (kind == K_ADJOINT || kind == K_ADJOINT_LEAN) ? h->geo_adj
                                                                        : h->geo;
@@ -615,27 +740,17 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   ALLOC(h->sens, (size_t)h->P * sizeof(double));
   ALLOC(h->partial, h->partial_cap * sizeof(double));
   ALLOC(h->counter, sizeof(unsigned));
-  // Inflow profile factors over each velocity boundary box, tabulated once:
-  // (m^2 - (y-m)^2)/m^2 with m = (ny-1)/2 (applications/diffuser/diffuser.cc:22-31),
-  // times the same in z on D3Q19.
+  // Inflow profile factors over each parabolic velocity boundary box,
+  // tabulated once (tables of LBM_PROFILE_TABLE boundaries come from
+  // lbm_set_bc_profile).
   for (int k = 0; k < c.nbc; ++k) {
     const lbm_bc& b = c.bc[k];
-    if (b.kind != LBM_BC_VELOCITY || b.profile != LBM_PROFILE_PARABOLIC) continue;
-    const int nyb = b.box[3] - b.box[2] + 1, nzb = b.box[5] - b.box[4] + 1;
-    std::vector<double> pd((size_t)nyb * nzb);
-    std::vector<float> pf(pd.size());
-    for (int z = b.box[4]; z <= b.box[5]; ++z)
-      for (int y = b.box[2]; y <= b.box[3]; ++y) {
-        double mid = (double)(c.ny - 1) / 2.;
-        double pr = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
-        if (h->dim == 3) {
-          double mz = (double)(h->cfg.nz - 1) / 2.;
-          pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
-        }
-        size_t i = (size_t)(z - b.box[4]) * nyb + (y - b.box[2]);
-        pd[i] = pr;
-        pf[i] = (float)pr;
-      }
+    if ((b.kind != LBM_BC_VELOCITY && b.kind != LBM_BC_VELOCITY_STANDARD) ||
+        b.profile != LBM_PROFILE_PARABOLIC)
+      continue;
+    std::vector<double> pd((size_t)bc_npos(b));
+    bc_parabola(c, b, pd.data());
+    std::vector<float> pf(pd.begin(), pd.end());
     ALLOC(h->bcprof_d[k], pd.size() * sizeof(double));
     ALLOC(h->bcprof_f[k], pf.size() * sizeof(float));
     cudaMemcpy(h->bcprof_d[k], pd.data(), pd.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -675,6 +790,55 @@ int lbm_get_sizes(const lbm_handle* h, int64_t* ncells, int* npop) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
   if (ncells) *ncells = h->ncell;
   if (npop) *npop = h->Q;
+  return LBM_OK;
+}
+
+int lbm_set_bc_profile(lbm_handle* h, int k, int nt, int ncomp, const double* table) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (k < 0 || k >= h->cfg.nbc) return fail(h, LBM_ERR_ARG, "boundary %d outside [0,%d)", k, h->cfg.nbc);
+  const lbm_bc& b = h->cfg.bc[k];
+  if (b.profile != LBM_PROFILE_TABLE)
+    return fail(h, LBM_ERR_STATE, "boundary %d was not configured with LBM_PROFILE_TABLE", k);
+  if (!table) return fail(h, LBM_ERR_ARG, "null table");
+  if (nt < 1) return fail(h, LBM_ERR_ARG, "table needs nt >= 1 rows");
+  const bool vel = b.kind == LBM_BC_VELOCITY || b.kind == LBM_BC_VELOCITY_STANDARD;
+  if (!(ncomp == 1 || (vel && ncomp == h->dim)))
+    return fail(h, LBM_ERR_ARG, "boundary %d: %d values per cell (1, or %d for a velocity)", k,
+                ncomp, h->dim);
+  const size_t n = (size_t)nt * (size_t)bc_npos(b) * (size_t)ncomp;
+  if (n > ((size_t)1 << 31)) return fail(h, LBM_ERR_ARG, "table of %zu values too large", n);
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(table[i])) return fail(h, LBM_ERR_NONFINITE, "table value %zu is not finite", i);
+  std::vector<float> tf(table, table + n);
+  const size_t old_n = h->bcprof_d[k] ? (size_t)(h->tab_nt[k] > 0 ? h->tab_nt[k] : 1) *
+                                            (size_t)bc_npos(b) *
+                                            (size_t)(h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1)
+                                      : 0;
+  // finish whatever still reads the old table before it changes (the handle's
+  // own stream, or the stream of a batch it belongs to)
+  CUDA_OR_FAIL(h, cudaDeviceSynchronize());
+  // captured graphs hold the table's address and layout: a new one needs a new capture
+  if (old_n != n || h->tab_nt[k] != nt || h->tab_ncomp[k] != ncomp) h->table_gen++;
+  if (old_n != n) {
+    if (h->bcprof_d[k]) cudaFree(h->bcprof_d[k]);
+    if (h->bcprof_f[k]) cudaFree(h->bcprof_f[k]);
+    h->bcprof_d[k] = nullptr;
+    h->bcprof_f[k] = nullptr;
+    h->tab_nt[k] = h->tab_ncomp[k] = 0;
+    cudaError_t e = cudaMalloc((void**)&h->bcprof_d[k], n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->bcprof_f[k], n * sizeof(float));
+    if (e != cudaSuccess) {
+      if (h->bcprof_d[k]) cudaFree(h->bcprof_d[k]);
+      h->bcprof_d[k] = nullptr;
+      h->bcprof_f[k] = nullptr;
+      return fail(h, e == cudaErrorMemoryAllocation ? LBM_ERR_MEM : LBM_ERR_CUDA,
+                  "table allocation: %s", cudaGetErrorString(e));
+    }
+  }
+  CUDA_OR_FAIL(h, cudaMemcpy(h->bcprof_d[k], table, n * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OR_FAIL(h, cudaMemcpy(h->bcprof_f[k], tf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  h->tab_nt[k] = nt;
+  h->tab_ncomp[k] = ncomp;
   return LBM_OK;
 }
 
@@ -1268,6 +1432,7 @@ struct lbm_batch {
   int grid_fwd = 1, grid_adj = 1, grid_obj = 1, grid_copy = 1;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = -1, graph_snap = -1, graph_schedule = -1;
+  int64_t graph_table_gen = -1;          // the lattices' table generations at capture
   int64_t graph_recomputed = 0;
   int64_t graph_launches = 0;            // kernels in the captured sequence
   int end_cur[LBM_MAX_BATCH] = {}, end_lcur[LBM_MAX_BATCH] = {};   // host state after it
@@ -1354,6 +1519,12 @@ void batch_set_grids(lbm_batch* b) {
 }
 
 int batch_launch(lbm_batch* b, int kind, const BatchParams& bp, int grid) {
+  for (int i = 0; i < b->n; ++i) {
+    const int k = bp.p[i].apply_bc ? missing_table(b->h[i]) : -1;
+    if (k >= 0)
+      return bfail(b, LBM_ERR_STATE, "lattice %d: boundary %d has LBM_PROFILE_TABLE but no table "
+                   "(lbm_set_bc_profile)", i, k);
+  }
   b->ops.launch(kind, dim3(grid), batch_block(b, kind), b->stream, bp);
   b->launches++;
   cudaError_t e = cudaGetLastError();
@@ -1555,6 +1726,7 @@ void batch_destroy_graph(lbm_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
   b->graph_steps = b->graph_snap = b->graph_schedule = -1;
+  b->graph_table_gen = -1;
 }
 
 }  // namespace
@@ -1830,8 +2002,10 @@ int lbm_batch_gradient_schedule(lbm_batch* b, int nsteps, int nsnap, int schedul
   int64_t recomputed = 0;
   cudaEventRecord(b->ev[0], b->stream);
   if (use_graph) {
+    int64_t table_gen = 0;
+    for (int i = 0; i < b->n; ++i) table_gen += b->h[i]->table_gen;
     if (!(b->graph && b->graph_steps == nsteps && b->graph_snap == nsnap &&
-          b->graph_schedule == schedule)) {
+          b->graph_schedule == schedule && b->graph_table_gen == table_gen)) {
       batch_destroy_graph(b);
       cudaGraph_t g = nullptr;
       const int64_t l0 = b->launches;
@@ -1853,6 +2027,7 @@ int lbm_batch_gradient_schedule(lbm_batch* b, int nsteps, int nsnap, int schedul
       b->graph_steps = nsteps;
       b->graph_snap = nsnap;
       b->graph_schedule = schedule;
+      b->graph_table_gen = table_gen;
       b->graph_recomputed = recomputed;
       for (int i = 0; i < b->n; ++i) {
         b->end_cur[i] = b->h[i]->cur;

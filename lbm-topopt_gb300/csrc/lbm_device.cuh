@@ -162,13 +162,17 @@ struct GammaT<double> {
 struct DevBC {
   int kind, face, profile;
   int box[6];
-  double value;       // value * (1 + amp sin(2 pi t / period)) at this launch's time t
+  int tang_x;         // 1: box cells ordered along x (south/north faces); 0: along y, then z
+  int n_t;            // box cells along the first tangential axis
+  int ncomp;          // table entries per cell: 0 (no table), 1 (factor), 2 or 3 (velocity vector)
+  double value;       // value * T(t) at this launch's time t
   float value_f;      // the same in FP32
   double vshift;      // value - 1 (pressure on shifted populations)
   float vshift_f;
-  const double* prof;   // inflow profile factor over the box, (z-z0)*ny_box + (y-y0); null = 1
+  double dir[3];      // velocity direction
+  float dir_f[3];
+  const double* prof;   // factor (or vector) table of this launch's time step over the box; null = 1
   const float* prof_f;
-  int ny_box;
 };
 
 template <class C>
@@ -184,14 +188,51 @@ __device__ __forceinline__ double bc_vshift<double>(const DevBC& b) { return b.v
 template <>
 __device__ __forceinline__ float bc_vshift<float>(const DevBC& b) { return b.vshift_f; }
 template <class C>
-__device__ __forceinline__ C bc_prof(const DevBC& b, int y, int z);
+__device__ __forceinline__ const C* bc_table(const DevBC& b);
 template <>
-__device__ __forceinline__ double bc_prof<double>(const DevBC& b, int y, int z) {
-  return b.prof ? b.prof[(z - b.box[4]) * b.ny_box + (y - b.box[2])] : 1.;
+__device__ __forceinline__ const double* bc_table<double>(const DevBC& b) { return b.prof; }
+template <>
+__device__ __forceinline__ const float* bc_table<float>(const DevBC& b) { return b.prof_f; }
+template <class C>
+__device__ __forceinline__ C bc_dir(const DevBC& b, int a);
+template <>
+__device__ __forceinline__ double bc_dir<double>(const DevBC& b, int a) { return b.dir[a]; }
+template <>
+__device__ __forceinline__ float bc_dir<float>(const DevBC& b, int a) { return b.dir_f[a]; }
+
+// Index of cell (x,y,z) among the box cells, in the order of the tables.
+__device__ __forceinline__ int bc_index(const DevBC& b, int x, int y, int z) {
+  return b.tang_x ? (x - b.box[0]) : ((z - b.box[4]) * b.n_t + (y - b.box[2]));
 }
-template <>
-__device__ __forceinline__ float bc_prof<float>(const DevBC& b, int y, int z) {
-  return b.prof_f ? b.prof_f[(z - b.box[4]) * b.ny_box + (y - b.box[2])] : 1.f;
+
+// Scalar value of a pressure or temperature boundary at a cell: value(t),
+// times the tabulated factor if there is one.
+template <class C>
+__device__ __forceinline__ C bc_scalar(const DevBC& b, int x, int y, int z) {
+  C v = bc_value<C>(b);
+  const C* t = bc_table<C>(b);
+  if (t) v *= t[bc_index(b, x, y, z)];
+  return v;
+}
+
+// Prescribed velocity at a cell: value(t) * profile * dir, or the tabulated
+// vector (the reference's Input functor, ZouHe2d.hh:37).
+template <class C>
+__device__ __forceinline__ void bc_velocity(const DevBC& b, int x, int y, int z, C& ux, C& uy,
+                                            C& uz) {
+  const C* t = bc_table<C>(b);
+  const int i = bc_index(b, x, y, z);
+  if (b.ncomp >= 2) {
+    ux = t[i * b.ncomp];
+    uy = t[i * b.ncomp + 1];
+    uz = b.ncomp == 3 ? t[i * b.ncomp + 2] : C(0.);
+    return;
+  }
+  C s = bc_value<C>(b);
+  if (t) s *= t[i];
+  ux = s * bc_dir<C>(b, 0);
+  uy = s * bc_dir<C>(b, 1);
+  uz = s * bc_dir<C>(b, 2);
 }
 
 // Model constants in one precision.  KParams carries an FP64 and an FP32 copy
@@ -222,6 +263,7 @@ struct KParams {
   // boundary conditions of the input state's time step
   int nbc;
   int apply_bc;
+  int bc_y;                // some boundary lies on a south or north face
   DevBC bc[LBM_MAX_BC];
   // objective
   int objective;
@@ -1576,8 +1618,25 @@ __device__ __forceinline__ void bgk_reverse_inc(const C* fin, const C* lam, C* d
 
 // ---------------------------------------------------------------------------
 // Boundary conditions on one cell's post-stream populations at time t.
-// Zou-He (boundaryConditions/ZouHe2d.hh:23-281), Hecht (Hecht3d.hh:62-94,175-209),
-// thermal Zou-He (thermalZouHe2d.hh:63-81).
+// Zou-He (boundaryConditions/ZouHe2d.hh:23-391), Hecht (Hecht3d.hh:62-94,175-209),
+// thermal Zou-He (thermalZouHe2d.hh:63-81).  D2Q9 numbering: e_1 = (1,-1),
+// e_2 = (0,-1), e_3 = (-1,-1), e_4 = (-1,0), e_5 = (-1,1), e_6 = (0,1),
+// e_7 = (1,1), e_8 = (1,0); a face's unknowns are the populations entering
+// from outside (west 1,7,8; east 3,4,5; north 1,2,3; south 5,6,7).
+//
+// On shifted storage (f - w) every relation below holds unchanged for the
+// deviations, because each one pairs populations of equal weight, except the
+// density sums: the known-population sums of the Zou-He density relations have
+// weight 1 (w_0 + w_2 + w_6 + 2(w_3 + w_4 + w_5) = 1 on the west face, and
+// alike on the others), so the shifted forms use rho0 - 1 (vshift) in place of
+// rho0, or add the 1 back where the density itself is needed.
+
+// Prescribed density of a pressure boundary in the storage's convention.
+template <bool SHIFT, class C>
+__device__ __forceinline__ C bc_rho(const DevBC& b, int x, int y, int z) {
+  if (bc_table<C>(b)) return bc_scalar<C>(b, x, y, z) - (SHIFT ? C(1.) : C(0.));
+  return SHIFT ? bc_vshift<C>(b) : bc_value<C>(b);
+}
 
 template <int LAT, bool SHIFT, class C>
 __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KParams& p) {
@@ -1585,13 +1644,20 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
   for (int k = 0; k < p.nbc; ++k) {
     const DevBC& b = p.bc[k];
     if (!in_box(b.box, x, y, z)) continue;
-    if (b.kind == LBM_BC_VELOCITY) {
-      // u = value(t) * profile(y, z) (profile tabulated at set-up, see DevBC)
-      C ux = bc_value<C>(b);
-      ux *= bc_prof<C>(b, y, z);
+    if (b.kind == LBM_BC_VELOCITY || b.kind == LBM_BC_VELOCITY_STANDARD) {
+      C ux, uy, uz;
+      bc_velocity<C>(b, x, y, z, ux, uy, uz);
       if (L::DIM == 2) {
-        const C uy = C(0.);
-        if (b.face == LBM_FACE_WEST) {
+        if (b.kind == LBM_BC_VELOCITY_STANDARD) {
+          // StandardZouHeVelocityWest2d (ZouHe2d.hh:146-163): the standard
+          // equilibrium's density from the known populations
+          C rho = (f[0] + f[2] + f[6] + C(2.) * (f[3] + f[4] + f[5]));
+          if (SHIFT) rho += C(1.);
+          rho = rho / (C(1.) - ux);
+          f[1] = f[5] + C(0.5) * (f[6] - f[2]) + C(1. / 6.) * rho * ux - C(0.5) * rho * uy;
+          f[7] = f[3] + C(0.5) * (f[2] - f[6]) + C(1. / 6.) * rho * ux + C(0.5) * rho * uy;
+          f[8] = f[4] + C(2. / 3.) * rho * ux;
+        } else if (b.face == LBM_FACE_WEST) {
           f[1] = C(0.5) * (f[6] - f[2]) + f[5] + C(1. / 6.) * ux - C(0.5) * uy;
           f[7] = C(0.5) * (f[2] - f[6]) + f[3] + C(1. / 6.) * ux + C(0.5) * uy;
           f[8] = f[4] + C(2. / 3.) * ux;
@@ -1599,23 +1665,45 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
           f[3] = f[7] + C(0.5) * (f[6] - f[2]) - C(1. / 6.) * ux - C(0.5) * uy;
           f[4] = f[8] - C(2. / 3.) * ux;
           f[5] = f[1] + C(0.5) * (f[2] - f[6]) - C(1. / 6.) * ux + C(0.5) * uy;
+        } else if (b.face == LBM_FACE_NORTH) {
+          // IncompressibleZouHeVelocityNorth2d (ZouHe2d.hh:66-81)
+          f[1] = C(0.5) * (f[4] - f[8]) + f[5] - C(1. / 6.) * uy + C(0.5) * ux;
+          f[2] = f[6] - C(2. / 3.) * uy;
+          f[3] = C(0.5) * (f[8] - f[4]) + f[7] - C(1. / 6.) * uy - C(0.5) * ux;
+        } else {
+          // south: the north operator mirrored in y (1<->7, 2<->6, 3<->5, uy -> -uy)
+          f[7] = C(0.5) * (f[4] - f[8]) + f[3] + C(1. / 6.) * uy + C(0.5) * ux;
+          f[6] = f[2] + C(2. / 3.) * uy;
+          f[5] = C(0.5) * (f[8] - f[4]) + f[1] + C(1. / 6.) * uy - C(0.5) * ux;
         }
       } else {
-        const C uy = C(0.), uz = C(0.);
-        if (b.face == LBM_FACE_WEST) {
-          C Nyx = C(0.5) * (f[5] + f[11] + f[13] - (f[2] + f[4] + f[14])) - C(1. / 3.) * uy;
-          C Nzx = C(0.5) * (f[10] + f[13] + f[14] - (f[1] + f[4] + f[5])) - C(1. / 3.) * uz;
-          f[7] = f[16] + C(1. / 6.) * (ux - uz) + Nzx;
-          f[9] = f[18] + C(1. / 6.) * (ux - uy) + Nyx;
-          f[12] = f[3] + C(1. / 3.) * ux;
-          f[15] = f[6] + C(1. / 6.) * (ux + uz) - Nzx;
-          f[17] = f[8] + C(1. / 6.) * (ux + uy) - Nyx;
-        }
+        C Nyx = C(0.5) * (f[5] + f[11] + f[13] - (f[2] + f[4] + f[14])) - C(1. / 3.) * uy;
+        C Nzx = C(0.5) * (f[10] + f[13] + f[14] - (f[1] + f[4] + f[5])) - C(1. / 3.) * uz;
+        f[7] = f[16] + C(1. / 6.) * (ux - uz) + Nzx;
+        f[9] = f[18] + C(1. / 6.) * (ux - uy) + Nyx;
+        f[12] = f[3] + C(1. / 3.) * ux;
+        f[15] = f[6] + C(1. / 6.) * (ux + uz) - Nzx;
+        f[17] = f[8] + C(1. / 6.) * (ux + uy) - Nyx;
       }
-    } else if (b.kind == LBM_BC_PRESSURE) {
-      const C rho0 = SHIFT ? bc_vshift<C>(b) : bc_value<C>(b);
+    } else if (b.kind == LBM_BC_PRESSURE || b.kind == LBM_BC_PRESSURE_STANDARD) {
+      const C rho0 = bc_rho<SHIFT, C>(b, x, y, z);
       if (L::DIM == 2) {
-        if (b.face == LBM_FACE_EAST) {
+        if (b.kind == LBM_BC_PRESSURE_STANDARD && !SHIFT) {
+          // StandardZouHePressureEast/West2d (ZouHe2d.hh:332-349, 366-383).  The
+          // map equals the incompressible one (rho0*ux0 = S - rho0); shifted
+          // storage evaluates it in that form below.
+          if (b.face == LBM_FACE_EAST) {
+            C ux0 = C(-1.) + (f[0] + f[2] + f[6] + C(2.) * (f[1] + f[7] + f[8])) / rho0;
+            f[4] = f[8] - C(2. / 3.) * rho0 * ux0;
+            f[3] = f[7] - C(1. / 6.) * rho0 * ux0 + C(0.5) * (f[6] - f[2]);
+            f[5] = f[1] - C(1. / 6.) * rho0 * ux0 + C(0.5) * (f[2] - f[6]);
+          } else {
+            C ux0 = C(1.) - (f[0] + f[2] + f[6] + C(2.) * (f[3] + f[4] + f[5])) / rho0;
+            f[1] = f[5] + C(1. / 6.) * rho0 * ux0 + C(0.5) * (f[6] - f[2]);
+            f[7] = f[3] + C(1. / 6.) * rho0 * ux0 + C(0.5) * (f[2] - f[6]);
+            f[8] = f[4] + C(2. / 3.) * rho0 * ux0;
+          }
+        } else if (b.face == LBM_FACE_EAST) {
           C ux0 = -rho0 + (f[0] + f[2] + f[6] + C(2.) * (f[1] + f[7] + f[8]));
           f[4] = f[8] - C(2. / 3.) * ux0;
           f[3] = f[7] - C(1. / 6.) * ux0 + C(0.5) * (f[6] - f[2]);
@@ -1625,8 +1713,20 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
           f[8] = f[4] + C(2. / 3.) * ux0;
           f[7] = f[3] + C(1. / 6.) * ux0 + C(0.5) * (f[2] - f[6]);
           f[1] = f[5] + C(1. / 6.) * ux0 + C(0.5) * (f[6] - f[2]);
+        } else if (b.face == LBM_FACE_NORTH) {
+          // the east operator rotated by +90 degrees (x -> y)
+          C uy0 = -rho0 + (f[0] + f[8] + f[4] + C(2.) * (f[7] + f[5] + f[6]));
+          f[2] = f[6] - C(2. / 3.) * uy0;
+          f[1] = f[5] - C(1. / 6.) * uy0 + C(0.5) * (f[4] - f[8]);
+          f[3] = f[7] - C(1. / 6.) * uy0 + C(0.5) * (f[8] - f[4]);
+        } else {
+          // south: the west operator rotated by +90 degrees
+          C uy0 = rho0 - (f[0] + f[8] + f[4] + C(2.) * (f[1] + f[2] + f[3]));
+          f[6] = f[2] + C(2. / 3.) * uy0;
+          f[5] = f[1] + C(1. / 6.) * uy0 + C(0.5) * (f[8] - f[4]);
+          f[7] = f[3] + C(1. / 6.) * uy0 + C(0.5) * (f[4] - f[8]);
         }
-      } else if (b.face == LBM_FACE_EAST) {
+      } else {
         C ux = f[0] + f[1] + f[2] + f[4] + f[5] + f[10] + f[11] + f[13] + f[14] +
                C(2.) * (f[7] + f[9] + f[12] + f[15] + f[17]) - rho0;
         C Nyx = C(0.5) * (f[5] + f[11] + f[13] - (f[2] + f[4] + f[14]));
@@ -1638,16 +1738,16 @@ __device__ __forceinline__ void apply_bcs(C* f, int x, int y, int z, const KPara
         f[18] = f[9] - C(1. / 6.) * ux - Nyx;
       }
     } else if (b.kind == LBM_BC_TEMPERATURE && LAT == LAT_D2Q9_D2Q5) {
-      if (b.face == LBM_FACE_WEST) {
-        C* g = f + 9;
-        g[4] = bc_value<C>(b) - g[0] - g[1] - g[2] - g[3];
-      }
+      C* g = f + 9;
+      g[4] = bc_scalar<C>(b, x, y, z) - g[0] - g[1] - g[2] - g[3];
     }
   }
 }
 
 // Transposes, applied in reverse order of the forward boundary loops
-// (adjointBoundaryConditions/adjointZouHe2d.cc:5-112, adjointHecht3d.cc:7-80).
+// (adjointBoundaryConditions/adjointZouHe2d.cc:5-112, adjointZouHe2d.hh:53-87,
+// adjointHecht3d.cc:7-80, adjointThermalZouHe2d.hh:56-71); the south velocity
+// and north/south pressure transposes follow from their forward operators.
 template <int LAT, class C>
 __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KParams& p) {
   using L = Lattice<LAT>;
@@ -1690,7 +1790,22 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
       }
       continue;
     }
-    if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) {
+    const bool pres = b.kind == LBM_BC_PRESSURE || b.kind == LBM_BC_PRESSURE_STANDARD;
+    if (b.kind == LBM_BC_VELOCITY_STANDARD) {
+      // AdjointStandardZouHeVelocityWest2d (adjointZouHe2d.hh:62-80)
+      C ux, uy, uz;
+      bc_velocity<C>(b, x, y, z, ux, uy, uz);
+      C adjRho = (C(1. / 6) * (ux / (C(1.) - ux)) - C(0.5) * (uy / (C(1.) - ux))) * a[1] +
+                 (C(1. / 6) * (ux / (C(1.) - ux)) + C(0.5) * (uy / (C(1.) - ux))) * a[7] +
+                 C(2. / 3.) * (ux / (C(1.) - ux)) * a[8];
+      a[0] += adjRho;
+      a[2] += C(0.5) * (a[7] - a[1]) + adjRho;
+      a[3] += a[7] + C(2.) * adjRho;
+      a[4] += a[8] + C(2.) * adjRho;
+      a[5] += a[1] + C(2.) * adjRho;
+      a[6] += C(0.5) * (a[1] - a[7]) + adjRho;
+      a[1] = a[7] = a[8] = C(0.);
+    } else if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_WEST) {
       a[2] += C(0.5) * (a[7] - a[1]);
       a[3] += a[7];
       a[4] += a[8];
@@ -1704,7 +1819,21 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
       a[7] += a[3];
       a[8] += a[4];
       a[3] = a[4] = a[5] = C(0.);
-    } else if (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_EAST) {
+    } else if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_NORTH) {
+      a[4] += C(0.5) * (a[1] - a[3]);
+      a[5] += a[1];
+      a[6] += a[2];
+      a[7] += a[3];
+      a[8] += C(0.5) * (a[3] - a[1]);
+      a[1] = a[2] = a[3] = C(0.);
+    } else if (b.kind == LBM_BC_VELOCITY && b.face == LBM_FACE_SOUTH) {
+      a[4] += C(0.5) * (a[7] - a[5]);
+      a[3] += a[7];
+      a[2] += a[6];
+      a[1] += a[5];
+      a[8] += C(0.5) * (a[5] - a[7]);
+      a[5] = a[6] = a[7] = C(0.);
+    } else if (pres && b.face == LBM_FACE_EAST) {
       C adjU = -C(1. / 6.) * a[3] - C(2. / 3.) * a[4] - C(1. / 6.) * a[5];
       a[0] += adjU;
       a[1] += C(2.) * adjU + a[5];
@@ -1713,7 +1842,7 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
       a[7] += C(2.) * adjU + a[3];
       a[8] += C(2.) * adjU + a[4];
       a[3] = a[4] = a[5] = C(0.);
-    } else if (b.kind == LBM_BC_PRESSURE && b.face == LBM_FACE_WEST) {
+    } else if (pres && b.face == LBM_FACE_WEST) {
       C adjU = C(1. / 6.) * a[1] + C(1. / 6.) * a[7] + C(2. / 3.) * a[8];
       a[0] -= adjU;
       a[2] -= adjU - C(0.5) * (a[7] - a[1]);
@@ -1722,6 +1851,24 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
       a[5] -= C(2.) * adjU - a[1];
       a[6] -= adjU - C(0.5) * (a[1] - a[7]);
       a[1] = a[7] = a[8] = C(0.);
+    } else if (pres && b.face == LBM_FACE_NORTH) {
+      C adjU = -C(1. / 6.) * a[1] - C(2. / 3.) * a[2] - C(1. / 6.) * a[3];
+      a[0] += adjU;
+      a[7] += C(2.) * adjU + a[3];
+      a[8] += adjU + C(0.5) * (a[3] - a[1]);
+      a[4] += adjU + C(0.5) * (a[1] - a[3]);
+      a[5] += C(2.) * adjU + a[1];
+      a[6] += C(2.) * adjU + a[2];
+      a[1] = a[2] = a[3] = C(0.);
+    } else if (pres && b.face == LBM_FACE_SOUTH) {
+      C adjU = C(1. / 6.) * a[7] + C(1. / 6.) * a[5] + C(2. / 3.) * a[6];
+      a[0] -= adjU;
+      a[8] -= adjU - C(0.5) * (a[5] - a[7]);
+      a[1] -= C(2.) * adjU - a[5];
+      a[2] -= C(2.) * adjU - a[6];
+      a[3] -= C(2.) * adjU - a[7];
+      a[4] -= adjU - C(0.5) * (a[7] - a[5]);
+      a[5] = a[6] = a[7] = C(0.);
     } else if (b.kind == LBM_BC_TEMPERATURE && b.face == LBM_FACE_WEST && LAT == LAT_D2Q9_D2Q5) {
       C* g = a + 9;
       g[0] -= g[4];
@@ -1730,185 +1877,6 @@ __device__ __forceinline__ void adjoint_bcs(C* a, int x, int y, int z, const KPa
       g[3] -= g[4];
       g[4] = C(0.);
     }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Objectives of one cell (value) and their partial derivatives.
-// PressureDrop2d (functionals/pressureDrop2d.hh:30-68), ThermalOutflowEast2d
-// (temperatureFlow2d.hh:106-142), dissipated power (no reference counterpart):
-// D = 2 alpha |j|^2 + (9/2) nu omega^2 sum_ab Pneq_ab^2.
-
-// component a of e_i
-template <class L>
-__host__ __device__ constexpr int lat_e(int i, int a) {
-  return a == 0 ? L::ex(i) : a == 1 ? L::ey(i) : L::ez(i);
-}
-
-// e_i^T P e_i for a symmetric 3x3 P, the zero terms left out (the rest in the
-// order a, b = 0..DIM-1)
-template <int LAT, int i, class C>
-__device__ __forceinline__ C e_quad(const C (&P)[3][3]) {
-  using L = Lattice<LAT>;
-  C v = C(0.);
-  static_for<L::DIM>([&](auto A) {
-    constexpr int a = decltype(A)::value;
-    static_for<L::DIM>([&](auto B) {
-      constexpr int b = decltype(B)::value;
-      constexpr int eab = lat_e<L>(i, a) * lat_e<L>(i, b);
-      if constexpr (eab == 1) v += P[a][b];
-      if constexpr (eab == -1) v -= P[a][b];
-    });
-  });
-  return v;
-}
-
-// P_ab = sum_i e_ia e_ib f_i over the flow lattice
-template <int LAT, class C>
-__device__ __forceinline__ void second_moment(const C* f, C (&P)[3][3]) {
-  using L = Lattice<LAT>;
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = 0; b < 3; ++b) P[a][b] = C(0.);
-  static_for<L::QF>([&](auto I) {
-    constexpr int i = decltype(I)::value;
-    static_for<L::DIM>([&](auto A) {
-      constexpr int a = decltype(A)::value;
-      static_for<L::DIM>([&](auto B) {
-        constexpr int b = decltype(B)::value;
-        constexpr int eab = lat_e<L>(i, a) * lat_e<L>(i, b);
-        if constexpr (eab == 1) P[a][b] += f[i];
-        if constexpr (eab == -1) P[a][b] -= f[i];
-      });
-    });
-  });
-}
-
-// Weighted objective of one cell, in the compute precision.  On shifted
-// storage the pressure drop sums rho - 1: the constant parts of the inflow and
-// outflow means cancel (weight*1 - weight*1).
-template <int LAT, bool SHIFT, class C>
-__device__ __forceinline__ C objective_cell(const C* f, C g, int x, int y, int z,
-                                            const KParams& p) {
-  using L = Lattice<LAT>;
-  if (p.objective == LBM_OBJ_PRESSURE_DROP) {
-    bool i1 = in_box(p.obj_in, x, y, z), i2 = in_box(p.obj_out, x, y, z);
-    if (!i1 && !i2) return C(0.);
-    C rho, jx, jy, jz;
-    flow_macros<LAT>(f, rho, jx, jy, jz);
-    C v = C(0.);
-    if (i1) v += mp<C>(p).w_in * rho;
-    if (i2) v -= mp<C>(p).w_out * rho;
-    return v;
-  }
-  if (p.objective == LBM_OBJ_OUTFLOW) {
-    if (!in_box(p.obj_out, x, y, z)) return C(0.);
-    C rho, jx, jy, jz;
-    flow_macros<LAT>(f, rho, jx, jy, jz);
-    return -mp<C>(p).w_out * jx;
-  }
-  if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
-    if (!in_box(p.obj_out, x, y, z)) return C(0.);
-    C rho, jx, jy, jz;
-    flow_macros<LAT>(f, rho, jx, jy, jz);
-    C T = f[9] + f[10] + f[11] + f[12] + f[13];
-    return -mp<C>(p).obj_weight * jx * T;
-  }
-  if (p.objective == LBM_OBJ_DISSIPATION) {
-    C rho, j[3];
-    flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
-    C P[3][3];
-    second_moment<LAT>(f, P);
-    C s2 = C(0.);
-#pragma unroll
-    for (int a = 0; a < L::DIM; ++a) {
-#pragma unroll
-      for (int b = 0; b < L::DIM; ++b) {
-        C v = P[a][b] - j[a] * j[b];
-        if (a == b) v -= rho / C(3.);
-        s2 += v * v;
-      }
-    }
-    const C cv = mp<C>(p).cv_diss;
-    const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
-    C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    return mp<C>(p).obj_weight * (C(2.) * alpha * jj + cv * s2);
-  }
-  return C(0.);
-}
-
-// lam += weight * dF/df ; dg += weight * dF/dgamma
-template <int LAT, bool SHIFT, class C>
-__device__ __forceinline__ void objective_source(const C* f, C g, C* lam, C& dg, int x, int y,
-                                                 int z, const KParams& p) {
-  using L = Lattice<LAT>;
-  if (p.objective == LBM_OBJ_PRESSURE_DROP) {
-    if (in_box(p.obj_in, x, y, z)) {
-      const C v = mp<C>(p).w_in;
-#pragma unroll
-      for (int d = 0; d < L::QF; ++d) lam[d] += v;
-    }
-    if (in_box(p.obj_out, x, y, z)) {
-      const C v = mp<C>(p).w_out;
-#pragma unroll
-      for (int d = 0; d < L::QF; ++d) lam[d] -= v;
-    }
-  } else if (p.objective == LBM_OBJ_OUTFLOW) {
-    if (in_box(p.obj_out, x, y, z)) {
-      const C v = mp<C>(p).w_out;
-      static_for<L::QF>([&](auto D) {
-        constexpr int d = decltype(D)::value;
-        if constexpr (L::ex(d) == 1) lam[d] -= v;
-        if constexpr (L::ex(d) == -1) lam[d] += v;
-      });
-    }
-  } else if (p.objective == LBM_OBJ_HEAT_FLUX && LAT == LAT_D2Q9_D2Q5) {
-    if (in_box(p.obj_out, x, y, z)) {
-      C rho, jx, jy, jz;
-      flow_macros<LAT>(f, rho, jx, jy, jz);
-      C T = f[9] + f[10] + f[11] + f[12] + f[13];
-      const C tc = mp<C>(p).obj_weight;
-      static_for<9>([&](auto D) {
-        constexpr int d = decltype(D)::value;
-        lam[d] -= tc * C(L::ex(d)) * T;
-      });
-#pragma unroll
-      for (int d = 9; d < 14; ++d) lam[d] -= tc * jx;
-    }
-  } else if (p.objective == LBM_OBJ_DISSIPATION) {
-    C rho, j[3];
-    flow_macros<LAT>(f, rho, j[0], j[1], j[2]);
-    C P[3][3];
-    second_moment<LAT>(f, P);
-    C tr = C(0.);
-#pragma unroll
-    for (int a = 0; a < L::DIM; ++a) {
-#pragma unroll
-      for (int b = 0; b < L::DIM; ++b) P[a][b] -= j[a] * j[b];
-      P[a][a] -= rho / C(3.);
-      tr += P[a][a];
-    }
-    // P j once; per population only the lattice vector's nonzero components
-    // (products with a zero component are not folded away in IEEE arithmetic)
-    C pj[3] = {C(0.), C(0.), C(0.)};
-#pragma unroll
-    for (int a = 0; a < L::DIM; ++a)
-#pragma unroll
-      for (int b = 0; b < L::DIM; ++b) pj[a] += P[a][b] * j[b];
-    const C cv = mp<C>(p).cv_diss;
-    const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
-    const C tc = mp<C>(p).obj_weight;
-    const C a4 = C(4.) * alpha, c2 = cv * C(2.), tr3 = tr / C(3.);
-    static_for<L::QF>([&](auto I) {
-      constexpr int i = decltype(I)::value;
-      const C ej = e_dot<LAT, i>(j[0], j[1], j[2]);
-      const C pej = e_dot<LAT, i>(pj[0], pj[1], pj[2]);   // e . P j
-      const C pe = e_quad<LAT, i>(P);                     // e . P e
-      lam[i] += tc * (a4 * ej + c2 * ((pe - tr3) - C(2.) * pej));
-    });
-    C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    dg += tc * (C(2.) * (C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q))) * jj);
   }
 }
 
@@ -2016,3 +1984,6 @@ __host__ __device__ inline unsigned batch_div_magic(unsigned long long d, unsign
 }
 
 }  // namespace lbm
+
+// The objectives, one functor each (LBMacroFunctional), used by the step kernels.
+#include "lbm_objectives.cuh"

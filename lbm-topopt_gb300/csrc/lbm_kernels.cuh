@@ -76,10 +76,11 @@ __device__ __forceinline__ bool interior(int x, int y, int z, const KParams& p) 
   return in;
 }
 
-// Boundary conditions only live on the x = 0 and x = nx-1 faces (checked
-// when the handle is created), so other cells skip the boundary loop.
-__device__ __forceinline__ bool on_bc_face(int x, const KParams& p) {
-  return p.apply_bc && (x == 0 || x == p.nx - 1);
+// Boundary conditions live on the x = 0 and x = nx-1 faces and, in 2D, on
+// the y = 0 and y = ny-1 faces (checked when the handle is created; p.bc_y
+// says whether any does), so other cells skip the boundary loop.
+__device__ __forceinline__ bool on_bc_face(int x, int y, const KParams& p) {
+  return p.apply_bc && (x == 0 || x == p.nx - 1 || (p.bc_y && (y == 0 || y == p.ny - 1)));
 }
 
 template <int LAT, class S>
@@ -186,7 +187,7 @@ __device__ __forceinline__ typename Store<S>::C forward_cell_from(const KParams&
   C objv = C(0.);
   {
     S* __restrict__ fout = (S*)p.fout;
-    if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     if (p.eval_obj) objv = objective_cell<LAT, SHIFT>(f, g, x, y, z, p);
     const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C rho, jx, jy, jz;
@@ -270,7 +271,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
   pull_all<LAT, A, C>(lam, lin, c, x, y, z, interior<LAT>(x, y, z, p), p);
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+  if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
   const C g = C(((const G*)p.gamma)[c]);
   const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
   const C dimult = C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q));
@@ -292,7 +293,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
       });
     }
     if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, d, dg, x, y, z, p);
-    if (on_bc_face(x, p)) {
+    if (on_bc_face(x, y, p)) {
       static_for<L::Q>([&](auto Q_) {
         constexpr int q = decltype(Q_)::value;
         lam[q] += d[q];
@@ -336,7 +337,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
     });
   }
   if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p);
-  if (on_bc_face(x, p)) adjoint_bcs<LAT>(lam, x, y, z, p);
+  if (on_bc_face(x, y, p)) adjoint_bcs<LAT>(lam, x, y, z, p);
   static_for<L::Q>([&](auto Q_) {
     constexpr int q = decltype(Q_)::value;
     lout[q * (int)p.P + c] = A(lam[q]);
@@ -357,7 +358,7 @@ __device__ __forceinline__ typename Store<S>::C objective_only_cell(const KParam
     const int c = (z * p.ny + y) * p.nx + x;
     C f[L::Q];
     load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-    if (on_bc_face(x, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     v = objective_cell<LAT, SHIFT>(f, C(((const G*)p.gamma)[c]), x, y, z, p);
   }
   return v;
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(256) k_export(KParams p, double* __restrict__ 
   const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  if (on_bc_face(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
   static_for<L::Q>([&](auto Q_) {
     constexpr int q = decltype(Q_)::value;
     aos[(long long)c * L::Q + q] = to_abs<LAT, S, q>(f[q]);
@@ -550,7 +551,7 @@ __global__ void __launch_bounds__(256) k_macros(KParams p, double* __restrict__ 
   const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  if (on_bc_face(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
   C rho, jx, jy, jz;
   flow_macros<LAT>(f, rho, jx, jy, jz);
   double* m = mac + (long long)c * L::NMAC;

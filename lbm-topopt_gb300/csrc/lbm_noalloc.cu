@@ -44,6 +44,12 @@ void* g_scratch_ptr[kMaxDevices] = {};
 double g_prof_d[kMaxProfile];
 float g_prof_f[kMaxProfile];
 
+// A velocity boundary whose factors this path tabulates into its scratch.
+bool parabolic(const lbm_bc& b) {
+  return (b.kind == LBM_BC_VELOCITY || b.kind == LBM_BC_VELOCITY_STANDARD) &&
+         b.profile == LBM_PROFILE_PARABOLIC;
+}
+
 int fail(int code, const std::string& msg) {
   lbm::set_global_error(msg.c_str());   // read back with lbm_last_error(NULL)
   return code;
@@ -81,8 +87,11 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
   long long nprof = 0;
   for (int k = 0; k < c.nbc; ++k) {
     const lbm_bc& b = c.bc[k];
-    if (b.kind == LBM_BC_VELOCITY && b.profile == LBM_PROFILE_PARABOLIC)
-      nprof += (long long)(b.box[3] - b.box[2] + 1) * (b.box[5] - b.box[4] + 1);
+    if (b.profile == LBM_PROFILE_TABLE)
+      return fail(LBM_ERR_SUP, "boundary " + std::to_string(k) +
+                                   ": tabulated profiles live in a handle; the allocation-free "
+                                   "path takes uniform and parabolic profiles only");
+    if (parabolic(b)) nprof += bc_npos(b);
   }
   if (nprof > kMaxProfile)
     return fail(LBM_ERR_ARG, "inflow profiles need " + std::to_string(nprof) +
@@ -138,14 +147,7 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
     p.obj_in[i] = c.obj_in[i];
     p.obj_out[i] = c.obj_out[i];
   }
-  if (c.objective == LBM_OBJ_PRESSURE_DROP) {
-    const int* a = c.obj_in;
-    p.inv_in = (double)(1. / ((a[1] - a[0] + 1) * (a[3] - a[2] + 1) * (a[5] - a[4] + 1)));
-  }
-  if (c.objective == LBM_OBJ_PRESSURE_DROP || c.objective == LBM_OBJ_OUTFLOW) {
-    const int* b = c.obj_out;
-    p.inv_out = (double)(1. / ((b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1)));
-  }
+  objective_norms(c, &p.inv_in, &p.inv_out);
   md.w_in = p.inv_in * c.obj_weight;
   md.w_out = p.inv_out * c.obj_weight;
   ModelParams<float>& mf = p.mf;
@@ -163,37 +165,14 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
   long long off = 0;
   for (int k = 0; k < c.nbc; ++k) {
     const lbm_bc& b = c.bc[k];
-    DevBC& d = p.bc[k];
-    d.kind = b.kind;
-    d.face = b.face;
-    d.profile = b.profile;
-    for (int i = 0; i < 6; ++i) d.box[i] = b.box[i];
-    double tf = (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
-    d.value = b.value * tf;
-    d.value_f = (float)d.value;
-    d.vshift = d.value - 1.;
-    d.vshift_f = (float)d.vshift;
-    d.ny_box = b.box[3] - b.box[2] + 1;
-    d.prof = nullptr;
-    d.prof_f = nullptr;
-    if (b.kind == LBM_BC_VELOCITY && b.profile == LBM_PROFILE_PARABOLIC) {
-      const int nyb = b.box[3] - b.box[2] + 1;
-      for (int z = b.box[4]; z <= b.box[5]; ++z)
-        for (int y = b.box[2]; y <= b.box[3]; ++y) {
-          double mid = (double)(c.ny - 1) / 2.;
-          double pr = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
-          if (dim == 3) {
-            double mz = (double)(nz - 1) / 2.;
-            pr *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
-          }
-          long long i = off + (long long)(z - b.box[4]) * nyb + (y - b.box[2]);
-          g_prof_d[i] = pr;
-          g_prof_f[i] = (float)pr;
-        }
-      d.prof = prof_d + off;
-      d.prof_f = prof_f + off;
-      off += (long long)nyb * (b.box[5] - b.box[4] + 1);
+    const bool par = parabolic(b);
+    if (par) {
+      bc_parabola(c, b, g_prof_d + off);
+      for (long long i = 0; i < bc_npos(b); ++i) g_prof_f[off + i] = (float)g_prof_d[off + i];
     }
+    fill_devbc(b, t, 1, par ? prof_d + off : nullptr, par ? prof_f + off : nullptr, p.bc[k]);
+    if (bc_on_y_face(b)) p.bc_y = 1;
+    if (par) off += bc_npos(b);
   }
   if (off > 0) {
     e = cudaMemcpyAsync(prof_d, g_prof_d, sizeof(double) * off, cudaMemcpyHostToDevice, st);

@@ -9,6 +9,8 @@ namespace lbm {
 
 struct KParams;
 struct BatchParams;
+struct DevBC;
+struct ObjectiveInfo;
 
 enum {
   K_FORWARD = 0,
@@ -47,5 +49,24 @@ LaunchFn launcher_thermal(int collision, int storage);
 void set_global_error(const char* msg);
 // The checks of lbm_create (message through lbm_last_error(NULL)); 0 = valid.
 int validate_config(const lbm_config& c);
+
+// Boundary conditions on the host.  Cells of b's box in table order (along the
+// face: y then z on west/east faces, x on south/north faces).
+int64_t bc_npos(const lbm_bc& b);
+// Whether b lies on a south or north face.
+bool bc_on_y_face(const lbm_bc& b);
+// T(t) of b's time law.
+double bc_time_factor(const lbm_bc& b, int t);
+// Parabolic factors of a velocity boundary over its box, bc_npos(b) values.
+void bc_parabola(const lbm_config& c, const lbm_bc& b, double* out);
+// Device parameters of boundary b at time step t.  tab_d / tab_f: the factor
+// (ncomp = 1) or velocity (ncomp = 2, 3) table row of step t, or null.
+void fill_devbc(const lbm_bc& b, int t, int ncomp, const double* tab_d, const float* tab_f,
+                DevBC& d);
+
+// The facts of objective `id` from the kernels' objective list; false if unknown.
+bool objective_info(int id, ObjectiveInfo* out);
+// 1/|in| and 1/|out| of the boxes the config's objective averages over (0 if unused).
+void objective_norms(const lbm_config& c, double* inv_in, double* inv_out);
 
 }  // namespace lbm

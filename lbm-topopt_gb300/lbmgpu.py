@@ -35,9 +35,12 @@ D2Q9, D3Q19, D2Q9_D2Q5 = 0, 1, 2
 BGK, MRT = 0, 1
 STORE_FP64, STORE_FP32, STORE_FP16 = 0, 1, 2
 BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE = 1, 2, 3
+BC_VELOCITY_STANDARD, BC_PRESSURE_STANDARD = 4, 5
 FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
-PROFILE_UNIFORM, PROFILE_PARABOLIC = 0, 1
+PROFILE_UNIFORM, PROFILE_PARABOLIC, PROFILE_TABLE = 0, 1, 2
+TIME_OFFSET_SINE, TIME_SINE = 0, 1
 OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX, OBJ_OUTFLOW = 0, 1, 2, 3, 4
+OBJ_THROUGH_FLOW = 5
 SCHEDULE_DYNAMIC, SCHEDULE_STATIC = 0, 1
 MAX_BC = 8
 
@@ -55,7 +58,7 @@ MRT2D_DEFAULT = (1.4, 1.4, 1.2, 0.0, 0.0, 0.0, 0.0, 0.0)
 class CBC(C.Structure):
     _fields_ = [("kind", C.c_int), ("face", C.c_int), ("profile", C.c_int),
                 ("box", C.c_int * 6), ("value", C.c_double), ("amp", C.c_double),
-                ("period", C.c_double)]
+                ("period", C.c_double), ("time_law", C.c_int), ("dir", C.c_double * 3)]
 
 
 class CConfig(C.Structure):
@@ -78,6 +81,9 @@ class CGradStats(C.Structure):
 
 @dataclass
 class Boundary:
+    """One ``lbm_bc``: value(t) = value * T(t) * profile, T(t) = 1 + amp sin(2 pi t /
+    period) (TIME_OFFSET_SINE) or amp sin(2 pi t / period) (TIME_SINE); a velocity
+    boundary imposes that times ``dir`` ((0,0,0) = +x)."""
     kind: int
     face: int
     box: Sequence[int]
@@ -85,6 +91,8 @@ class Boundary:
     profile: int = PROFILE_UNIFORM
     amp: float = 0.0
     period: float = 1.0
+    time_law: int = TIME_OFFSET_SINE
+    dir: Sequence[float] = (0.0, 0.0, 0.0)
 
 
 @dataclass
@@ -148,6 +156,9 @@ class Config:
             for i in range(6):
                 cb.box[i] = int(b.box[i])
             cb.value, cb.amp, cb.period = b.value, b.amp, b.period
+            cb.time_law = b.time_law
+            for i in range(3):
+                cb.dir[i] = float(b.dir[i])
         c.objective = self.objective
         for i in range(6):
             c.obj_in[i] = int(self.obj_in[i])
@@ -183,6 +194,7 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_last_error": (C.c_char_p, [H]),
         "lbm_get_sizes": (C.c_int, [H, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
         "lbm_set_design": (C.c_int, [H, dp]),
+        "lbm_set_bc_profile": (C.c_int, [H, C.c_int, C.c_int, C.c_int, dp]),
         "lbm_init_equilibrium": (C.c_int, [H, dp]),
         "lbm_forward": (C.c_int, [H, C.c_int, dp, dp]),
         "lbm_get_time": (C.c_int, [H, C.POINTER(C.c_int)]),
@@ -363,6 +375,19 @@ class Handle:
             raise LBMError(rc, self.lib.lbm_last_error(self.h).decode())
 
     # -- forward ---------------------------------------------------------------
+    def set_bc_profile(self, k: int, table):
+        """Table of boundary k (configured with PROFILE_TABLE): shape (nt, npos)
+        for a factor, (nt, npos, dim) for a velocity vector; row t mod nt is used
+        at time step t (lbm_set_bc_profile)."""
+        a = np.ascontiguousarray(table, dtype=np.float64)
+        if a.ndim == 2:
+            nt, ncomp = a.shape[0], 1
+        elif a.ndim == 3:
+            nt, ncomp = a.shape[0], a.shape[2]
+        else:
+            raise ValueError("table must be (nt, npos) or (nt, npos, ncomp)")
+        self._check(self.lib.lbm_set_bc_profile(self.h, int(k), int(nt), int(ncomp), _ptr(a)))
+
     def set_design(self, gamma: np.ndarray):
         g = np.ascontiguousarray(gamma, dtype=np.float64).ravel()
         if g.size != self.cfg.ncells:

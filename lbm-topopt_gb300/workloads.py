@@ -19,8 +19,9 @@ import math
 import numpy as np
 
 from lbmgpu import (BC_PRESSURE, BC_TEMPERATURE, BC_VELOCITY, BGK, D2Q9, D2Q9_D2Q5, D3Q19,
-                    FACE_EAST, FACE_WEST, MRT, OBJ_DISSIPATION, OBJ_HEAT_FLUX,
-                    OBJ_PRESSURE_DROP, PROFILE_PARABOLIC, STORE_FP64, Boundary, Config)
+                    FACE_EAST, FACE_NORTH, FACE_WEST, MRT, OBJ_DISSIPATION, OBJ_HEAT_FLUX,
+                    OBJ_PRESSURE_DROP, OBJ_THROUGH_FLOW, PROFILE_PARABOLIC, PROFILE_TABLE,
+                    STORE_FP64, TIME_SINE, Boundary, Config)
 
 SEED_BASE = 20261203
 MASK64 = (1 << 64) - 1
@@ -120,6 +121,43 @@ def thermal_2d(nx: int, ny: int, *, tau: float = 0.8, u0: float = 0.03, du: floa
              Boundary(BC_PRESSURE, FACE_EAST, outlet, 1.0),
              Boundary(BC_TEMPERATURE, FACE_WEST, inlet, 0.0)],
         objective=OBJ_HEAT_FLUX, obj_in=inlet, obj_out=outlet, obj_weight=1.0 / nsteps)
+
+
+def pump_2d(n: int, *, tau: float = 0.8, u_max: float = 0.05, period: float = 200.0,
+            alpha_max: float = 0.05, q: float = 0.1, collision: int = MRT,
+            storage: int = STORE_FP64, nsteps: int = 600) -> Config:
+    """The robust pump's set-up (applications/RobustPump2d/robustPump2d.cc:52-104) on an
+    n x n lattice, n divisible by 3, th = n/3: Zou-He pressure rho = 1 on the west
+    and east segments y = th+1..2th, a north Zou-He velocity inlet on x =
+    th+1..2th with the zero-mean oscillation u_y(t) = -u_max sin(2 pi t/period) p(x)
+    (p from ``pump_inflow_profile``, the reference's InflowVelocity), and the
+    through-flow objective over the two pressure segments (ThroughFlow2d,
+    robustPump2d.cc:165-166).  The reference closes the rest of the box with
+    on-grid bounce-back; here the pull stream's mid-way bounce-back walls do."""
+    th = n // 3
+    west = (0, 0, th + 1, 2 * th, 0, 0)
+    east = (n - 1, n - 1, th + 1, 2 * th, 0, 0)
+    north = (th + 1, 2 * th, n - 1, n - 1, 0, 0)
+    return Config(
+        lattice=D2Q9, collision=collision, storage=storage, nx=n, ny=n, nz=1,
+        omega=1.0 / tau, mrt=(1.4, 1.4, 1.2, 0, 0, 0, 0, 0),
+        interp_scale=2.0 * alpha_max, interp_q=q,
+        bcs=[Boundary(BC_PRESSURE, FACE_WEST, west, 1.0),
+             Boundary(BC_PRESSURE, FACE_EAST, east, 1.0),
+             Boundary(BC_VELOCITY, FACE_NORTH, north, u_max, PROFILE_TABLE, 1.0, period,
+                      TIME_SINE, (0.0, -1.0, 0.0))],
+        objective=OBJ_THROUGH_FLOW, obj_in=west, obj_out=east, obj_weight=1.0 / nsteps)
+
+
+def pump_inflow_profile(cfg: Config) -> np.ndarray:
+    """Factors (r^2 - (x - mid)^2) / r^2 of the north inlet cells x = th+1..2th, mid
+    = (n-1)/2, r = th/2 (the InflowVelocity of robustPump2d.cc:13-25), as the one-row
+    table of ``lbm_set_bc_profile`` (shape (1, th))."""
+    n = cfg.nx
+    th = n // 3
+    mid, r = (n - 1) / 2.0, th / 2.0
+    x = np.arange(th + 1, 2 * th + 1, dtype=np.float64)
+    return ((r * r - (x - mid) * (x - mid)) / (r * r))[None, :]
 
 
 def thermal_design(nx: int, ny: int, seed: int) -> np.ndarray:

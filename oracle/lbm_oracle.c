@@ -727,16 +727,56 @@ static void adjoint_stream_all(const model_t* m, const double* src, double* dst)
 /* Boundary conditions */
 
 static double time_factor(const lbm_bc* b, int t) {
+  if (b->time_law == LBM_TIME_SINE)
+    return b->amp == 0. ? 0. : b->amp * sin(2. * M_PI * (double)t / b->period);
   if (b->amp == 0.) return 1.;
   return 1. + b->amp * sin(2. * M_PI * (double)t / b->period);
 }
 
-/* Velocity profile at (y,z): the reference applications' inflow functors
- * (applications/diffuser/diffuser.cc:22-31): ux = vmax*(mid^2-(y-mid)^2)/mid^2. */
-static double profile(const model_t* m, const lbm_bc* b, int y, int z) {
+/* Tabulated boundary inputs (the library's lbm_set_bc_profile), one per
+ * boundary slot: nt rows of npos cells of ncomp values. */
+static struct {
+  double* v;
+  int nt, ncomp;
+  int64_t npos;
+} g_tab[LBM_MAX_BC];
+
+static int on_y_face(const lbm_bc* b) {
+  return b->face == LBM_FACE_SOUTH || b->face == LBM_FACE_NORTH;
+}
+
+int orc_set_bc_profile(int k, int nt, int ncomp, int64_t npos, const double* table) {
+  if (k < 0 || k >= LBM_MAX_BC) return -1;
+  free(g_tab[k].v);
+  g_tab[k].v = NULL;
+  g_tab[k].nt = g_tab[k].ncomp = 0;
+  g_tab[k].npos = 0;
+  if (!table) return 0;
+  size_t n = (size_t)nt * (size_t)npos * (size_t)ncomp;
+  g_tab[k].v = (double*)malloc(sizeof(double) * n);
+  if (!g_tab[k].v) return -4;
+  memcpy(g_tab[k].v, table, sizeof(double) * n);
+  g_tab[k].nt = nt;
+  g_tab[k].ncomp = ncomp;
+  g_tab[k].npos = npos;
+  return 0;
+}
+
+/* Index of (x,y,z) among the box cells: along y, then z, on west/east faces;
+ * along x on south/north faces. */
+static int64_t bc_index(const lbm_bc* b, int x, int y, int z) {
+  if (on_y_face(b)) return x - b->box[0];
+  return (int64_t)(z - b->box[4]) * (b->box[3] - b->box[2] + 1) + (y - b->box[2]);
+}
+
+/* Velocity profile along the face: the reference applications' inflow
+ * functors (applications/diffuser/diffuser.cc:22-31): vmax*(mid^2-(s-mid)^2)/mid^2
+ * across the lattice (s = y on west/east faces, x on south/north faces). */
+static double profile(const model_t* m, const lbm_bc* b, int x, int y, int z) {
   if (b->profile != LBM_PROFILE_PARABOLIC) return 1.;
-  double mid = (double)(m->ny - 1) / 2.;
-  double p = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
+  int n = on_y_face(b) ? m->nx : m->ny, s = on_y_face(b) ? x : y;
+  double mid = (double)(n - 1) / 2.;
+  double p = (mid * mid - (s - mid) * (s - mid)) / (mid * mid);
   if (m->dim == 3) {
     double mz = (double)(m->nz - 1) / 2.;
     p *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
@@ -744,24 +784,61 @@ static double profile(const model_t* m, const lbm_bc* b, int y, int z) {
   return p;
 }
 
-static double bc_value(const model_t* m, const lbm_bc* b, int t, int y, int z) {
+static const double* table_entry(const lbm_bc* b, int k, int t, int x, int y, int z) {
+  if (b->profile != LBM_PROFILE_TABLE || !g_tab[k].v) return NULL;
+  return g_tab[k].v + ((int64_t)(t % g_tab[k].nt) * g_tab[k].npos + bc_index(b, x, y, z)) *
+                          g_tab[k].ncomp;
+}
+
+/* Scalar value (density, temperature) of boundary k at a cell. */
+static double bc_scalar(const model_t* m, int k, int t, int x, int y, int z) {
+  const lbm_bc* b = &m->cfg.bc[k];
   double v = b->value * time_factor(b, t);
-  if (b->kind == LBM_BC_VELOCITY) v *= profile(m, b, y, z);
+  const double* e = table_entry(b, k, t, x, y, z);
+  if (e) v *= e[0];
   return v;
 }
 
-/* IncompressibleZouHeVelocityWest/North/East2d<D2Q9> (boundaryConditions/ZouHe2d.hh:29-44,66-81,
- * 103-118) and IncompressibleZouHePressureEast/West2d<D2Q9> (ZouHe2d.hh:245-281, 292-…). */
-static void zouhe2d(const model_t* m, const lbm_bc* b, int t, double* F) {
+/* Velocity of boundary k at a cell: value * T(t) * profile * dir, or the
+ * tabulated vector. */
+static void bc_velocity(const model_t* m, int k, int t, int x, int y, int z, double* u) {
+  const lbm_bc* b = &m->cfg.bc[k];
+  const double* e = table_entry(b, k, t, x, y, z);
+  if (e && g_tab[k].ncomp >= 2) {
+    u[0] = e[0];
+    u[1] = e[1];
+    u[2] = g_tab[k].ncomp == 3 ? e[2] : 0.;
+    return;
+  }
+  double v = b->value * time_factor(b, t);
+  v *= e ? e[0] : profile(m, b, x, y, z);
+  int nodir = b->dir[0] == 0. && b->dir[1] == 0. && b->dir[2] == 0.;
+  for (int a = 0; a < 3; ++a) u[a] = v * (nodir ? (a == 0 ? 1. : 0.) : b->dir[a]);
+}
+
+/* Zou-He boundaries of D2Q9 (boundaryConditions/ZouHe2d.hh):
+ * IncompressibleZouHeVelocityWest/North/East2d (:29-44, 66-81, 103-118),
+ * StandardZouHeVelocityWest2d (:146-163), IncompressibleZouHePressureEast/West2d
+ * (:252-268, 292-308), StandardZouHePressureEast/West2d (:332-349, 366-383); the
+ * south velocity is the north one mirrored in y, the north and south pressures
+ * the east and west ones rotated by +90 degrees (no reference counterparts). */
+static void zouhe2d(const model_t* m, int k, int t, double* F) {
+  const lbm_bc* b = &m->cfg.bc[k];
   int Q = m->Q;
   for (int z = b->box[4]; z <= b->box[5]; ++z)
     for (int y = b->box[2]; y <= b->box[3]; ++y)
       for (int x = b->box[0]; x <= b->box[1]; ++x) {
         double* f = F + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
-        double v = bc_value(m, b, t, y, z);
-        if (b->kind == LBM_BC_VELOCITY) {
-          double ux = v, uy = 0.;
-          if (b->face == LBM_FACE_WEST) {
+        if (b->kind == LBM_BC_VELOCITY || b->kind == LBM_BC_VELOCITY_STANDARD) {
+          double u[3];
+          bc_velocity(m, k, t, x, y, z, u);
+          double ux = u[0], uy = u[1];
+          if (b->kind == LBM_BC_VELOCITY_STANDARD) {
+            double rho = (f[0] + f[2] + f[6] + 2. * (f[3] + f[4] + f[5])) / (1. - ux);
+            f[1] = f[5] + 0.5 * (f[6] - f[2]) + (1. / 6.) * rho * ux - 0.5 * rho * uy;
+            f[7] = f[3] + 0.5 * (f[2] - f[6]) + (1. / 6.) * rho * ux + 0.5 * rho * uy;
+            f[8] = f[4] + (2. / 3.) * rho * ux;
+          } else if (b->face == LBM_FACE_WEST) {
             f[1] = 0.5 * (f[6] - f[2]) + f[5] + (1. / 6.) * ux - 0.5 * uy;
             f[7] = 0.5 * (f[2] - f[6]) + f[3] + (1. / 6.) * ux + 0.5 * uy;
             f[8] = f[4] + (2. / 3.) * ux;
@@ -770,15 +847,27 @@ static void zouhe2d(const model_t* m, const lbm_bc* b, int t, double* F) {
             f[4] = f[8] - (2. / 3.) * ux;
             f[5] = f[1] + 0.5 * (f[2] - f[6]) - (1. / 6.) * ux + 0.5 * uy;
           } else if (b->face == LBM_FACE_NORTH) {
-            /* velocity tangential ux along the lid, uy = 0 */
-            double vx = v, vy = 0.;
-            f[1] = 0.5 * (f[4] - f[8]) + f[5] - (1. / 6.) * vy + 0.5 * vx;
-            f[2] = f[6] - (2. / 3.) * vy;
-            f[3] = 0.5 * (f[8] - f[4]) + f[7] - (1. / 6.) * vy - 0.5 * vx;
+            f[1] = 0.5 * (f[4] - f[8]) + f[5] - (1. / 6.) * uy + 0.5 * ux;
+            f[2] = f[6] - (2. / 3.) * uy;
+            f[3] = 0.5 * (f[8] - f[4]) + f[7] - (1. / 6.) * uy - 0.5 * ux;
+          } else {
+            f[7] = 0.5 * (f[4] - f[8]) + f[3] + (1. / 6.) * uy + 0.5 * ux;
+            f[6] = f[2] + (2. / 3.) * uy;
+            f[5] = 0.5 * (f[8] - f[4]) + f[1] + (1. / 6.) * uy - 0.5 * ux;
           }
-        } else if (b->kind == LBM_BC_PRESSURE) {
-          double rho0 = v, ux0;
-          if (b->face == LBM_FACE_EAST) {
+        } else if (b->kind == LBM_BC_PRESSURE || b->kind == LBM_BC_PRESSURE_STANDARD) {
+          double rho0 = bc_scalar(m, k, t, x, y, z), ux0;
+          if (b->kind == LBM_BC_PRESSURE_STANDARD && b->face == LBM_FACE_EAST) {
+            ux0 = -1. + (f[0] + f[2] + f[6] + 2. * (f[1] + f[7] + f[8])) / rho0;
+            f[4] = f[8] - (2. / 3.) * rho0 * ux0;
+            f[3] = f[7] - (1. / 6.) * rho0 * ux0 + 0.5 * (f[6] - f[2]);
+            f[5] = f[1] - (1. / 6.) * rho0 * ux0 + 0.5 * (f[2] - f[6]);
+          } else if (b->kind == LBM_BC_PRESSURE_STANDARD) {
+            ux0 = 1. - (f[0] + f[2] + f[6] + 2. * (f[3] + f[4] + f[5])) / rho0;
+            f[1] = f[5] + (1. / 6.) * rho0 * ux0 + 0.5 * (f[6] - f[2]);
+            f[7] = f[3] + (1. / 6.) * rho0 * ux0 + 0.5 * (f[2] - f[6]);
+            f[8] = f[4] + (2. / 3.) * rho0 * ux0;
+          } else if (b->face == LBM_FACE_EAST) {
             ux0 = -rho0 + (f[0] + f[2] + f[6] + 2. * (f[1] + f[7] + f[8]));
             f[4] = f[8] - (2. / 3.) * ux0;
             f[3] = f[7] - (1. / 6.) * ux0 + 0.5 * (f[6] - f[2]);
@@ -788,26 +877,38 @@ static void zouhe2d(const model_t* m, const lbm_bc* b, int t, double* F) {
             f[8] = f[4] + (2. / 3.) * ux0;
             f[7] = f[3] + (1. / 6.) * ux0 + 0.5 * (f[2] - f[6]);
             f[1] = f[5] + (1. / 6.) * ux0 + 0.5 * (f[6] - f[2]);
+          } else if (b->face == LBM_FACE_NORTH) {
+            double uy0 = -rho0 + (f[0] + f[8] + f[4] + 2. * (f[7] + f[5] + f[6]));
+            f[2] = f[6] - (2. / 3.) * uy0;
+            f[1] = f[5] - (1. / 6.) * uy0 + 0.5 * (f[4] - f[8]);
+            f[3] = f[7] - (1. / 6.) * uy0 + 0.5 * (f[8] - f[4]);
+          } else {
+            double uy0 = rho0 - (f[0] + f[8] + f[4] + 2. * (f[1] + f[2] + f[3]));
+            f[6] = f[2] + (2. / 3.) * uy0;
+            f[5] = f[1] + (1. / 6.) * uy0 + 0.5 * (f[8] - f[4]);
+            f[7] = f[3] + (1. / 6.) * uy0 + 0.5 * (f[4] - f[8]);
           }
         } else if (b->kind == LBM_BC_TEMPERATURE) {
           /* ThermalZouHeWest2d<.,D2Q5,.> (boundaryConditions/thermalZouHe2d.hh:63-81) */
           double* g = f + 9;
-          if (b->face == LBM_FACE_WEST) g[4] = v - g[0] - g[1] - g[2] - g[3];
+          if (b->face == LBM_FACE_WEST) g[4] = bc_scalar(m, k, t, x, y, z) - g[0] - g[1] - g[2] - g[3];
         }
       }
 }
 
 /* IncompressibleHechtVelocityWest3d<D3Q19> (boundaryConditions/Hecht3d.hh:62-94) and
  * IncompressibleHechtPressureEast3d<D3Q19> (Hecht3d.hh:175-209). */
-static void hecht3d(const model_t* m, const lbm_bc* b, int t, double* F) {
+static void hecht3d(const model_t* m, int k, int t, double* F) {
+  const lbm_bc* b = &m->cfg.bc[k];
   int Q = m->Q;
   for (int z = b->box[4]; z <= b->box[5]; ++z)
     for (int y = b->box[2]; y <= b->box[3]; ++y)
       for (int x = b->box[0]; x <= b->box[1]; ++x) {
         double* fd = F + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
-        double v = bc_value(m, b, t, y, z);
         if (b->kind == LBM_BC_VELOCITY && b->face == LBM_FACE_WEST) {
-          double ux = v, uy = 0., uz = 0.;
+          double u[3];
+          bc_velocity(m, k, t, x, y, z, u);
+          double ux = u[0], uy = u[1], uz = u[2];
           double Nyx = 0.5 * (fd[5] + fd[11] + fd[13] - (fd[2] + fd[4] + fd[14])) - (1. / 3.) * uy;
           double Nzx = 0.5 * (fd[10] + fd[13] + fd[14] - (fd[1] + fd[4] + fd[5])) - (1. / 3.) * uz;
           fd[7] = fd[16] + (1. / 6.) * (ux - uz) + Nzx;
@@ -816,7 +917,7 @@ static void hecht3d(const model_t* m, const lbm_bc* b, int t, double* F) {
           fd[15] = fd[6] + (1. / 6.) * (ux + uz) - Nzx;
           fd[17] = fd[8] + (1. / 6.) * (ux + uy) - Nyx;
         } else if (b->kind == LBM_BC_PRESSURE && b->face == LBM_FACE_EAST) {
-          double rho0 = v;
+          double rho0 = bc_scalar(m, k, t, x, y, z);
           double ux = fd[0] + fd[1] + fd[2] + fd[4] + fd[5] + fd[10] + fd[11] + fd[13] + fd[14] +
                       2. * (fd[7] + fd[9] + fd[12] + fd[15] + fd[17]) - rho0;
           double Nyx = 0.5 * (fd[5] + fd[11] + fd[13] - (fd[2] + fd[4] + fd[14]));
@@ -832,11 +933,10 @@ static void hecht3d(const model_t* m, const lbm_bc* b, int t, double* F) {
 
 static void apply_bcs(const model_t* m, int t, double* F) {
   for (int k = 0; k < m->cfg.nbc; ++k) {
-    const lbm_bc* b = &m->cfg.bc[k];
     if (m->dim == 3)
-      hecht3d(m, b, t, F);
+      hecht3d(m, k, t, F);
     else
-      zouhe2d(m, b, t, F);
+      zouhe2d(m, k, t, F);
   }
 }
 
@@ -896,7 +996,25 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             }
             continue;
           }
-          if (b->kind == LBM_BC_VELOCITY && b->face == LBM_FACE_WEST) {
+          int pres = b->kind == LBM_BC_PRESSURE || b->kind == LBM_BC_PRESSURE_STANDARD;
+          if (b->kind == LBM_BC_VELOCITY_STANDARD) {
+            /* AdjointStandardZouHeVelocityWest2d (adjointZouHe2d.hh:62-80) */
+            double u[3];
+            bc_velocity(m, k, t, x, y, z, u);
+            double ux = u[0], uy = u[1];
+            double adjRho = ((1. / 6) * (ux / (1. - ux)) - 0.5 * (uy / (1. - ux))) * a[1] +
+                            ((1. / 6) * (ux / (1. - ux)) + 0.5 * (uy / (1. - ux))) * a[7] +
+                            (2. / 3.) * (ux / (1. - ux)) * a[8];
+            a[0] += adjRho;
+            a[2] += 0.5 * (a[7] - a[1]) + adjRho;
+            a[3] += a[7] + 2. * adjRho;
+            a[4] += a[8] + 2. * adjRho;
+            a[5] += a[1] + 2. * adjRho;
+            a[6] += 0.5 * (a[1] - a[7]) + adjRho;
+            a[1] = 0.;
+            a[7] = 0.;
+            a[8] = 0.;
+          } else if (b->kind == LBM_BC_VELOCITY && b->face == LBM_FACE_WEST) {
             a[2] += 0.5 * (a[7] - a[1]);
             a[3] += a[7];
             a[4] += a[8];
@@ -914,6 +1032,15 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             a[1] = 0.;
             a[2] = 0.;
             a[3] = 0.;
+          } else if (b->kind == LBM_BC_VELOCITY && b->face == LBM_FACE_SOUTH) {
+            a[4] += 0.5 * (a[7] - a[5]);
+            a[3] += a[7];
+            a[2] += a[6];
+            a[1] += a[5];
+            a[8] += 0.5 * (a[5] - a[7]);
+            a[5] = 0.;
+            a[6] = 0.;
+            a[7] = 0.;
           } else if (b->kind == LBM_BC_VELOCITY && b->face == LBM_FACE_EAST) {
             a[1] += a[5];
             a[2] += 0.5 * (a[5] - a[3]);
@@ -923,7 +1050,7 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             a[3] = 0.;
             a[4] = 0.;
             a[5] = 0.;
-          } else if (b->kind == LBM_BC_PRESSURE && b->face == LBM_FACE_EAST) {
+          } else if (pres && b->face == LBM_FACE_EAST) {
             double adjU = -(1. / 6.) * a[3] - (2. / 3.) * a[4] - (1. / 6.) * a[5];
             a[0] += adjU;
             a[1] += 2. * adjU + a[5];
@@ -934,7 +1061,7 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             a[3] = 0.;
             a[4] = 0.;
             a[5] = 0.;
-          } else if (b->kind == LBM_BC_PRESSURE && b->face == LBM_FACE_WEST) {
+          } else if (pres && b->face == LBM_FACE_WEST) {
             double adjU = (1. / 6.) * a[1] + (1. / 6.) * a[7] + (2. / 3.) * a[8];
             a[0] -= adjU;
             a[2] -= adjU - 0.5 * (a[7] - a[1]);
@@ -945,6 +1072,28 @@ static void adjoint_bcs(const model_t* m, int t, double* A) {
             a[1] = 0.;
             a[7] = 0.;
             a[8] = 0.;
+          } else if (pres && b->face == LBM_FACE_NORTH) {
+            double adjU = -(1. / 6.) * a[1] - (2. / 3.) * a[2] - (1. / 6.) * a[3];
+            a[0] += adjU;
+            a[7] += 2. * adjU + a[3];
+            a[8] += adjU + 0.5 * (a[3] - a[1]);
+            a[4] += adjU + 0.5 * (a[1] - a[3]);
+            a[5] += 2. * adjU + a[1];
+            a[6] += 2. * adjU + a[2];
+            a[1] = 0.;
+            a[2] = 0.;
+            a[3] = 0.;
+          } else if (pres && b->face == LBM_FACE_SOUTH) {
+            double adjU = (1. / 6.) * a[7] + (1. / 6.) * a[5] + (2. / 3.) * a[6];
+            a[0] -= adjU;
+            a[8] -= adjU - 0.5 * (a[5] - a[7]);
+            a[1] -= 2. * adjU - a[5];
+            a[2] -= 2. * adjU - a[6];
+            a[3] -= 2. * adjU - a[7];
+            a[4] -= adjU - 0.5 * (a[7] - a[5]);
+            a[5] = 0.;
+            a[6] = 0.;
+            a[7] = 0.;
           } else if (b->kind == LBM_BC_TEMPERATURE && b->face == LBM_FACE_WEST) {
             double* g = a + 9;
             g[0] -= g[4];
@@ -1055,6 +1204,28 @@ static double objective(const model_t* m, const double* F, const double* gamma) 
           of -= tc * invOut * mac[1];
         }
     return of;
+  } else if (c->objective == LBM_OBJ_THROUGH_FLOW) {
+    /* ThroughFlow2d::evaluate (functionals/throughFlow2d.hh:17-40) */
+    double invIn = (double)(1. / box_count(c->obj_in));
+    double invOut = (double)(1. / box_count(c->obj_out));
+    double iif = 0., of = 0.;
+    const int* b = c->obj_in;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double mac[4];
+          flow_macros(m, F + (((int64_t)z * m->ny + y) * m->nx + x) * Q, mac);
+          iif -= tc * invIn * mac[1];
+        }
+    b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double mac[4];
+          flow_macros(m, F + (((int64_t)z * m->ny + y) * m->nx + x) * Q, mac);
+          of -= tc * invOut * mac[1];
+        }
+    return iif + of;
   } else if (c->objective == LBM_OBJ_HEAT_FLUX) {
     double pout = 0.;
     const int* b = c->obj_out;
@@ -1104,6 +1275,24 @@ static void objective_source(const model_t* m, const double* F, const double* ga
     /* OutflowEast2d::adjointCollideSource, incompressible macros (outflow2d.hh:28-40) */
     double invOut = (double)(1. / box_count(c->obj_out));
     const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
+          for (int d = 0; d < m->Qf; ++d) a[d] -= invOut * tc * m->L->ex[d];
+        }
+  } else if (c->objective == LBM_OBJ_THROUGH_FLOW) {
+    /* ThroughFlow2d::adjointCollideSource, incompressible macros (throughFlow2d.hh:41-59) */
+    double invIn = (double)(1. / box_count(c->obj_in));
+    double invOut = (double)(1. / box_count(c->obj_out));
+    const int* b = c->obj_in;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
+          for (int d = 0; d < m->Qf; ++d) a[d] -= invIn * tc * m->L->ex[d];
+        }
+    b = c->obj_out;
     for (int z = b[4]; z <= b[5]; ++z)
       for (int y = b[2]; y <= b[3]; ++y)
         for (int x = b[0]; x <= b[1]; ++x) {

@@ -43,6 +43,10 @@ int orc_static_count(int nsteps, int nsnap, int64_t* recomputed, int* ok, int* s
 int orc_time_steps(const lbm_config* cfg, const double* gamma, int nsteps, int nthreads,
                    double* sec_fwd, double* sec_adj);
 int orc_max_threads(void);
+/* Table of boundary slot k for configs whose boundary k has LBM_PROFILE_TABLE
+ * (the library's lbm_set_bc_profile): nt rows of npos cells of ncomp values;
+ * table = NULL clears the slot.  Process-wide, like the test that sets it. */
+int orc_set_bc_profile(int k, int nt, int ncomp, int64_t npos, const double* table);
 
 #ifdef __cplusplus
 }

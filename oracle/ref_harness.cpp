@@ -96,14 +96,19 @@ struct MRT3dAdapter : public IncompressibleMRT3d<D3Q19, double, C> {
 };
 
 double time_factor(const lbm_bc& b, int t) {
+  if (b.time_law == LBM_TIME_SINE) return b.amp == 0. ? 0. : b.amp * sin(2. * M_PI * (double)t / b.period);
   if (b.amp == 0.) return 1.;
   return 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
 }
 
-double profile(const lbm_config& c, const lbm_bc& b, int y, int z) {
+/* parabola across the lattice along the face (s = y on west/east faces, x on
+ * south/north faces), times the same in z in 3D */
+double profile(const lbm_config& c, const lbm_bc& b, int x, int y, int z) {
   if (b.profile != LBM_PROFILE_PARABOLIC) return 1.;
-  double mid = (double)(c.ny - 1) / 2.;
-  double p = (mid * mid - (y - mid) * (y - mid)) / (mid * mid);
+  const bool yface = b.face == LBM_FACE_SOUTH || b.face == LBM_FACE_NORTH;
+  const int n = yface ? c.nx : c.ny, s = yface ? x : y;
+  double mid = (double)(n - 1) / 2.;
+  double p = (mid * mid - (s - mid) * (s - mid)) / (mid * mid);
   if (c.lattice == LBM_D3Q19) {
     double mz = (double)(c.nz - 1) / 2.;
     p *= (mz * mz - (z - mz) * (z - mz)) / (mz * mz);
@@ -111,24 +116,85 @@ double profile(const lbm_config& c, const lbm_bc& b, int y, int z) {
   return p;
 }
 
+/* Tabulated inputs per boundary slot (the library's lbm_set_bc_profile): nt
+ * rows of npos cells of ncomp values, cells along the face. */
+struct Table {
+  std::vector<double> v;
+  int nt = 0, ncomp = 0;
+  long long npos = 0;
+};
+Table g_tables[LBM_MAX_BC];
+
+const double* table_entry(const lbm_bc& b, int k, int t, int i, int j) {
+  if (b.profile != LBM_PROFILE_TABLE) return nullptr;
+  const Table& tb = g_tables[k];
+  if (tb.v.empty()) throw 4;
+  const bool yface = b.face == LBM_FACE_SOUTH || b.face == LBM_FACE_NORTH;
+  const long long pos = yface ? i - b.box[0] : j - b.box[2];
+  return tb.v.data() + ((long long)(t % tb.nt) * tb.npos + pos) * tb.ncomp;
+}
+
+/* The Input functors the reference's Zou-He loops call (ZouHe2d.hh:37):
+ * velocity value * T(t) * profile * dir (or a tabulated vector), density
+ * value * T(t) (times a tabulated factor). */
 struct VelFunc {
   lbm_config c;
   lbm_bc b;
-  void operator()(PetscInt t, PetscInt, PetscInt j, PetscScalar& ux, PetscScalar& uy) const {
+  int k;
+  void operator()(PetscInt t, PetscInt i, PetscInt j, PetscScalar& ux, PetscScalar& uy) const {
+    const double* e = table_entry(b, k, (int)t, (int)i, (int)j);
+    if (e && g_tables[k].ncomp >= 2) {
+      ux = e[0];
+      uy = e[1];
+      return;
+    }
     double v = b.value * time_factor(b, t);
-    v *= profile(c, b, j, 0);
-    ux = v;
-    uy = 0.;
+    v *= e ? e[0] : profile(c, b, i, j, 0);
+    const bool nodir = b.dir[0] == 0. && b.dir[1] == 0. && b.dir[2] == 0.;
+    ux = v * (nodir ? 1. : b.dir[0]);
+    uy = v * (nodir ? 0. : b.dir[1]);
   }
 };
 
 struct PresFunc {
   lbm_config c;
   lbm_bc b;
-  void operator()(PetscInt t, PetscInt, PetscInt, PetscScalar& rho) const {
+  int k;
+  void operator()(PetscInt t, PetscInt i, PetscInt j, PetscScalar& rho) const {
     rho = b.value * time_factor(b, t);
+    const double* e = table_entry(b, k, (int)t, (int)i, (int)j);
+    if (e) rho *= e[0];
   }
 };
+
+/* The reference's boundary loop for b (and its adjoint loop, null where the
+ * reference has none: the standard pressure boundaries, LBBoundaryLoop.cc:11-18);
+ * throws for boundaries the reference does not have. */
+void make_zouhe(const lbm_config& c, int k, LBBoundaryLoop** l, AdjointLBBoundaryLoop** al) {
+  const lbm_bc& b = c.bc[k];
+  Box2d bb(b.box[0], b.box[1], b.box[2], b.box[3]);
+  *l = nullptr;
+  *al = nullptr;
+  if (b.kind == LBM_BC_VELOCITY) {
+    VelFunc vf{c, b, k};
+    if (b.face == LBM_FACE_WEST) *l = new IncompressibleZouHeVelocityWest2d<D2Q9, VelFunc>(bb, vf);
+    if (b.face == LBM_FACE_EAST) *l = new IncompressibleZouHeVelocityEast2d<D2Q9, VelFunc>(bb, vf);
+    if (b.face == LBM_FACE_NORTH) *l = new IncompressibleZouHeVelocityNorth2d<D2Q9, VelFunc>(bb, vf);
+  } else if (b.kind == LBM_BC_VELOCITY_STANDARD) {
+    VelFunc vf{c, b, k};
+    if (b.face == LBM_FACE_WEST) *l = new StandardZouHeVelocityWest2d<D2Q9, VelFunc>(bb, vf);
+  } else if (b.kind == LBM_BC_PRESSURE) {
+    PresFunc pf{c, b, k};
+    if (b.face == LBM_FACE_EAST) *l = new IncompressibleZouHePressureEast2d<D2Q9, PresFunc>(bb, pf);
+    if (b.face == LBM_FACE_WEST) *l = new IncompressibleZouHePressureWest2d<D2Q9, PresFunc>(bb, pf);
+  } else if (b.kind == LBM_BC_PRESSURE_STANDARD) {
+    PresFunc pf{c, b, k};
+    if (b.face == LBM_FACE_EAST) *l = new StandardZouHePressureEast2d<D2Q9, PresFunc>(bb, pf);
+    if (b.face == LBM_FACE_WEST) *l = new StandardZouHePressureWest2d<D2Q9, PresFunc>(bb, pf);
+  }
+  if (!*l) throw 1;
+  if ((*l)->getAdjointBoundaryLoop(al)) *al = nullptr;
+}
 
 /* T*** / T**** views over contiguous AoS storage, as DMDAVecGetArrayDOF gives. */
 struct View2 {
@@ -174,22 +240,10 @@ struct Sim2d {
       : c(cfg), nx(cfg.nx), ny(cfg.ny), op(base, ScaledBP(cfg.interp_q, cfg.interp_scale)),
         box(0, cfg.nx - 1, 0, cfg.ny - 1) {
     for (int k = 0; k < c.nbc; ++k) {
-      const lbm_bc& b = c.bc[k];
-      Box2d bb(b.box[0], b.box[1], b.box[2], b.box[3]);
-      LBBoundaryLoop* l = nullptr;
-      if (b.kind == LBM_BC_VELOCITY) {
-        VelFunc vf{c, b};
-        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHeVelocityWest2d<D2Q9, VelFunc>(bb, vf);
-        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHeVelocityEast2d<D2Q9, VelFunc>(bb, vf);
-      } else if (b.kind == LBM_BC_PRESSURE) {
-        PresFunc pf{c, b};
-        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHePressureEast2d<D2Q9, PresFunc>(bb, pf);
-        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHePressureWest2d<D2Q9, PresFunc>(bb, pf);
-      }
-      if (!l) throw 1;
+      LBBoundaryLoop* l;
+      AdjointLBBoundaryLoop* al;
+      make_zouhe(c, k, &l, &al);
       bcs.emplace_back(l);
-      AdjointLBBoundaryLoop* al = nullptr;
-      if (l->getAdjointBoundaryLoop(&al)) throw 2;
       abcs.emplace_back(al);
     }
   }
@@ -225,6 +279,17 @@ struct Sim2d {
 
   double functional(const std::vector<double>& mac) {
     double tc = c.obj_weight, ps = 0.;
+    if (c.objective == LBM_OBJ_THROUGH_FLOW) {
+      /* ThroughFlow2d::evaluate (functionals/throughFlow2d.hh:17-40), one rank */
+      double invIn = box_inv(c.obj_in), invOut = box_inv(c.obj_out), iif = 0., of = 0.;
+      for (int j = c.obj_in[2]; j <= c.obj_in[3]; ++j)
+        for (int i = c.obj_in[0]; i <= c.obj_in[1]; ++i)
+          iif -= tc * invIn * mac[((size_t)j * nx + i) * 3 + 1];
+      for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
+        for (int i = c.obj_out[0]; i <= c.obj_out[1]; ++i)
+          of -= tc * invOut * mac[((size_t)j * nx + i) * 3 + 1];
+      return iif + of;
+    }
     if (c.objective == LBM_OBJ_OUTFLOW) {
       double inv = box_inv(c.obj_out), of = 0.;
       for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
@@ -244,6 +309,17 @@ struct Sim2d {
   }
 
   void source(std::vector<double>& adj) {
+    if (c.objective == LBM_OBJ_THROUGH_FLOW) {
+      /* ThroughFlow2d::adjointCollideSource, incompressible macros (throughFlow2d.hh:41-59) */
+      double tc = c.obj_weight, invIn = box_inv(c.obj_in), invOut = box_inv(c.obj_out);
+      for (int j = c.obj_in[2]; j <= c.obj_in[3]; ++j)
+        for (int i = c.obj_in[0]; i <= c.obj_in[1]; ++i)
+          for (int d = 0; d < 9; ++d) adj[((size_t)j * nx + i) * 9 + d] -= invIn * tc * D2Q9::ex[d];
+      for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
+        for (int i = c.obj_out[0]; i <= c.obj_out[1]; ++i)
+          for (int d = 0; d < 9; ++d) adj[((size_t)j * nx + i) * 9 + d] -= invOut * tc * D2Q9::ex[d];
+      return;
+    }
     if (c.objective == LBM_OBJ_OUTFLOW) {
       double tc = c.obj_weight, inv = box_inv(c.obj_out);
       for (int j = c.obj_out[2]; j <= c.obj_out[3]; ++j)
@@ -271,7 +347,10 @@ struct Sim2d {
     SourceAdjointObstIsoCollisionLoop2d<Op, decltype(rop)> aloop(box, rop);
     aloop.execute(va.p, vf.p, vg.p, vs.p);
     source(adj);
-    for (auto& b : abcs) b->execute(t, va.p, vf.p);
+    for (auto& b : abcs) {
+      if (!b) throw 2;   /* a boundary without an adjoint in the reference */
+      b->execute(t, va.p, vf.p);
+    }
     std::vector<double> al = adj;
     View2 vl(al.data(), nx, ny, Q);
     AdjointIsoStreamingLoop2d<Op> sloop(box, box);
@@ -322,9 +401,12 @@ struct Sim3d {
         for (int y = b.box[2]; y <= b.box[3]; ++y) {
           double* fd = &f[idx(b.box[0], y, z) * Q];
           double v = b.value * time_factor(b, t);
+          if (b.profile == LBM_PROFILE_TABLE) throw 4;
           if (b.kind == LBM_BC_VELOCITY) {
-            v *= profile(c, b, y, z);
-            double ux = v, uy = 0., uz = 0.;
+            v *= profile(c, b, b.box[0], y, z);
+            const bool nodir = b.dir[0] == 0. && b.dir[1] == 0. && b.dir[2] == 0.;
+            double ux = v * (nodir ? 1. : b.dir[0]), uy = v * (nodir ? 0. : b.dir[1]),
+                   uz = v * (nodir ? 0. : b.dir[2]);
             double Nyx = 0.5 * (fd[5] + fd[11] + fd[13] - (fd[2] + fd[4] + fd[14])) - (1. / 3.) * uy;
             double Nzx = 0.5 * (fd[10] + fd[13] + fd[14] - (fd[1] + fd[4] + fd[5])) - (1. / 3.) * uz;
             fd[7] = fd[16] + (1. / 6.) * (ux - uz) + Nzx;
@@ -463,25 +545,17 @@ struct SimThermal {
     if (cfg.heat_rate != 0.) throw 3;
     for (int k = 0; k < c.nbc; ++k) {
       const lbm_bc& b = c.bc[k];
-      Box2d bb(b.box[0], b.box[1], b.box[2], b.box[3]);
-      LBBoundaryLoop* l = nullptr;
-      AdjointLBBoundaryLoop* al = nullptr;
-      if (b.kind == LBM_BC_VELOCITY) {
-        VelFunc vf{c, b};
-        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHeVelocityWest2d<D2Q9, VelFunc>(bb, vf);
-        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHeVelocityEast2d<D2Q9, VelFunc>(bb, vf);
-      } else if (b.kind == LBM_BC_PRESSURE) {
-        PresFunc pf{c, b};
-        if (b.face == LBM_FACE_EAST) l = new IncompressibleZouHePressureEast2d<D2Q9, PresFunc>(bb, pf);
-        if (b.face == LBM_FACE_WEST) l = new IncompressibleZouHePressureWest2d<D2Q9, PresFunc>(bb, pf);
-      } else if (b.kind == LBM_BC_TEMPERATURE && b.face == LBM_FACE_WEST) {
+      if (b.kind == LBM_BC_TEMPERATURE && b.face == LBM_FACE_WEST) {
+        if (b.profile == LBM_PROFILE_TABLE) throw 4;
         tbcs.push_back(b);
-        abcs.emplace_back(new AdjointThermalZouHeWest2d<D2Q9, D2Q5>(bb));
+        abcs.emplace_back(new AdjointThermalZouHeWest2d<D2Q9, D2Q5>(
+            Box2d(b.box[0], b.box[1], b.box[2], b.box[3])));
         continue;
       }
-      if (!l) throw 1;
+      LBBoundaryLoop* l;
+      AdjointLBBoundaryLoop* al;
+      make_zouhe(c, k, &l, &al);
       bcs.emplace_back(l);
-      if (l->getAdjointBoundaryLoop(&al)) throw 2;
       abcs.emplace_back(al);
     }
   }
@@ -567,7 +641,10 @@ struct SimThermal {
     SourceAdjointObstThermalCollisionLoop2d<Op, decltype(rop)> aloop(box, rop);
     aloop.execute(va.p, vf.p, vg.p, vs.p);
     source(adj, f);
-    for (auto& b : abcs) b->execute(t, va.p, vf.p);
+    for (auto& b : abcs) {
+      if (!b) throw 2;
+      b->execute(t, va.p, vf.p);
+    }
     std::vector<double> al = adj;
     adjoint_stream_lattice<D2Q9>(adj, al, 0);
     adjoint_stream_lattice<D2Q5>(adj, al, 9);
@@ -708,6 +785,21 @@ class CountingStatic : public StaticCheckpointing {
 }  // namespace
 
 extern "C" {
+
+/* Table of boundary slot k (see Table); table = NULL clears it. */
+int ref_set_bc_profile(int k, int nt, int ncomp, long long npos, const double* table) {
+  if (k < 0 || k >= LBM_MAX_BC) return -1;
+  Table& tb = g_tables[k];
+  tb.v.clear();
+  tb.nt = tb.ncomp = 0;
+  tb.npos = 0;
+  if (!table) return 0;
+  tb.v.assign(table, table + (size_t)nt * (size_t)npos * (size_t)ncomp);
+  tb.nt = nt;
+  tb.ncomp = ncomp;
+  tb.npos = npos;
+  return 0;
+}
 
 int ref_forward(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
                 double* f_out, double* J_steps, double* J_sum) {

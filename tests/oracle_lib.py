@@ -34,6 +34,9 @@ def _bind(lib, prefix):
     for k, (r, a) in sig.items():
         fn = getattr(lib, prefix + k)
         fn.restype, fn.argtypes = r, a
+    fn = getattr(lib, prefix + "set_bc_profile")
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64 if prefix == "orc_" else C.c_longlong, _dp]
     if prefix == "orc_":
         lib.orc_wang_count.restype = C.c_int
         lib.orc_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
@@ -71,6 +74,19 @@ class OracleLib:
 
     def _fn(self, name):
         return getattr(self.lib, self.prefix + name)
+
+    def set_tables(self, tables=None):
+        """Tables of LBM_PROFILE_TABLE boundaries, {slot: (nt, npos) or (nt, npos,
+        ncomp) array}, as the library's lbm_set_bc_profile takes them; None
+        clears every slot."""
+        for k in range(8):
+            self._fn("set_bc_profile")(k, 0, 0, 0, None)
+        for k, t in (tables or {}).items():
+            a = np.ascontiguousarray(t, dtype=np.float64)
+            ncomp = 1 if a.ndim == 2 else a.shape[2]
+            rc = self._fn("set_bc_profile")(int(k), a.shape[0], ncomp, a.shape[1], _p(a))
+            if rc:
+                raise RuntimeError("set_bc_profile failed: %d" % rc)
 
     def forward(self, cfg: Config, gamma, nsteps, macros=None):
         c = cfg.to_c()

@@ -17,21 +17,66 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 
-@pytest.fixture(scope="module")
-def driver():
+def _build(name):
     if shutil.which("g++") is None:
         pytest.skip("needs g++")
     d = tempfile.mkdtemp()
-    exe = os.path.join(d, "cpp_driver")
+    exe = os.path.join(d, name)
     subprocess.check_call(["g++", "-std=c++14", "-O2", "-Wall", "-Werror",
-                           os.path.join(HERE, "cpp_driver.cpp"), "-o", exe,
+                           os.path.join(HERE, name + ".cpp"), "-o", exe,
                            "-L" + os.path.dirname(G.LIB_PATH), "-llbmgpu",
                            "-Wl,-rpath," + os.path.dirname(G.LIB_PATH)])
     return exe, d
 
 
+@pytest.fixture(scope="module")
+def driver():
+    return _build("cpp_driver")
+
+
+@pytest.fixture(scope="module")
+def pump_driver():
+    return _build("cpp_pump_driver")
+
+
 def test_cpp_driver_builds(driver):
     assert os.path.exists(driver[0])
+
+
+def test_cpp_pump_driver_builds(pump_driver):
+    assert os.path.exists(pump_driver[0])
+
+
+@pytest.mark.gpu
+def test_cpp_pump_driver_with_a_reference_style_input_functor(pump_driver, orc):
+    """The pump set-up with the reference's InflowVelocity law as a C++ functor
+    (tabulated by the facade) against the oracle given the same velocities."""
+    exe, d = pump_driver
+    n, nsteps, freq = 36, 150, 50
+    gamma = W.design_2d(n, n, 32)
+    path = os.path.join(d, "gamma.bin")
+    gamma.tofile(path)
+    out = subprocess.run([exe, str(n), str(nsteps), str(freq), path], capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = {ln.split()[0]: ln.split()[1:] for ln in out.stdout.splitlines()}
+    J = float(lines["J"][0])
+    sens = np.array([float(v) for v in lines["sens"]])
+    cfg = W.pump_2d(n, nsteps=nsteps, period=float(freq))
+    cfg.bcs[2] = G.Boundary(G.BC_VELOCITY, G.FACE_NORTH, cfg.bcs[2].box, 1.0, G.PROFILE_TABLE)
+    th = n // 3
+    x = np.arange(th + 1, 2 * th + 1, dtype=np.float64)
+    mid, r = (n - 1) / 2.0, th / 2.0
+    vec = np.zeros((freq, th, 2))
+    for t in range(freq):
+        vec[t, :, 1] = -np.sin(2.0 * np.pi * t / freq) * (0.05 * (r * r - (x - mid) ** 2)) / (r * r)
+    orc.set_tables({2: vec})
+    try:
+        Jo, so = orc.gradient(cfg, gamma, nsteps)
+    finally:
+        orc.set_tables(None)
+    assert abs(J - Jo) <= 1e-12 * abs(Jo)
+    assert rel_inf(sens, so) < 1e-11
 
 
 @pytest.mark.gpu
