@@ -104,6 +104,12 @@ extern "C" {
 #define LBM_TIME_SINE        1  /* T(t) = amp*sin(2*pi*t/period): zero mean, e.g. the
                                    oscillating pump inlet of applications/RobustPump2d/
                                    robustPump2d.cc:13-25 */
+#define LBM_TIME_RAMP        2  /* T(t) = amp + r(t - t_s), r(s) = 0 for s <= 0,
+                                   sin(pi s / (2 period)) for 0 < s < period, 1 after;
+                                   t_s = the step at which the last steady phase ended
+                                   (lbm_forward_steady, lbm_gradient_steady), never before
+                                   one: the StageTemp input of applications/Regenerator2d/
+                                   regenerator2d.cc:53-69 (T0 = value*amp, dT = value) */
 
 /* Objectives (functionals/LBMacroFunctional.hh:6-14). */
 #define LBM_OBJ_NONE          0
@@ -113,6 +119,12 @@ extern "C" {
 #define LBM_OBJ_OUTFLOW       4  /* -(mean u_x over obj_out): functionals/outflow2d.hh:10-54 */
 #define LBM_OBJ_THROUGH_FLOW  5  /* -(mean u_x over obj_in + mean u_x over obj_out):
                                     functionals/throughFlow2d.hh:17-83 */
+#define LBM_OBJ_DOMAIN_TEMPERATURE 6  /* mean T over obj_out (thermal lattice):
+                                         functionals/domainTemperature2d.hh:13-40 */
+#define LBM_OBJ_REGENERATOR_EFFICIENCY 7  /* sum (1-gamma)(T - Ti) / sum (1-gamma)(Tb - Ti)
+                                             over obj_out, Ti = obj_param[0], Tb = obj_param[1]
+                                             (thermal lattice): functionals/
+                                             regeneratorEfficiency2d.hh:16-88 */
 
 /* One boundary condition: the reference's boundary loop plus its Input
  * functor (ZouHe2d.hh:37: velocity or density as a function of the time step
@@ -161,6 +173,7 @@ typedef struct lbm_config {
   int obj_in[6];       /* inflow box of the pressure drop */
   int obj_out[6];      /* outflow box (pressure drop, heat flux) */
   double obj_weight;   /* timeConst: weight of each step's value (1/N for a time average) */
+  double obj_param[4]; /* objective parameters (LBM_OBJ_REGENERATOR_EFFICIENCY: Ti, Tb) */
 } lbm_config;
 
 typedef struct lbm_handle lbm_handle;
@@ -307,6 +320,24 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnapshots, double* J,
  * gradient does not depend on the schedule (recomputation is bit-exact). */
 int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnapshots, int schedule, double* J,
                           double* dJdgamma, lbm_gradient_stats* stats);
+
+/* The regenerator applications' gradient (applications/Regenerator2d/
+ * regenerator2d.cc:266-387, ComputeObjectiveAndSens): from f_0 (uniform rest or
+ * the macros of the last lbm_init_equilibrium), run to a steady state -- every
+ * check_every steps the largest change of any population over the last step,
+ * max |f_t - f_{t-1}|, is measured; the phase ends when it is below tol or
+ * after max_steady steps -- then n_unsteady more steps whose states' objective
+ * is summed (J = sum_{t=S+1..S+n_unsteady} weight*F(f_t), S = the steady
+ * steps).  LBM_TIME_RAMP boundaries start their ramp at step S (StageTemp,
+ * regenerator2d.cc:53-69).  The reverse sweep runs through all S + n_unsteady
+ * steps, the steady part without objective source (the reference's
+ * EmptyFunctional), closed by the reverse of the collision of f_0; the states
+ * come from Wang et al. dynamic checkpointing in nsnapshots device slots (the
+ * length of the sweep is not known in advance).  *steady_steps (may be NULL)
+ * gets S; J, dJdgamma and stats as for lbm_gradient. */
+int lbm_gradient_steady(lbm_handle* h, int max_steady, int check_every, double tol,
+                        int n_unsteady, int nsnapshots, int* steady_steps, double* J,
+                        double* dJdgamma, lbm_gradient_stats* stats);
 
 /* Device-time measurement for benchmarks: run `nsteps` forward steps
  * (which = 0), reverse steps over the current state (which = 1; the forward
@@ -505,11 +536,20 @@ int lbm_topopt_update(lbm_topopt* t, double* change, double* constraints);
  *             ready when the stream is.
  * Its scratch (block partial sums, a counter, inflow-profile tables) is one
  * fixed 640 KiB array per GPU, held for the life of the process.  Limits:
- * at most 8,388,608 cells and 32,768 tabulated inflow-profile values; larger
- * requests return LBM_ERR_ARG.  Every call shares that array, so calls that
- * overlap on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  The first call on each device looks up the
- * array's device address; make that call before any stream capture.
+ * at most 32,768 thread blocks of 256 threads, ceil(nx/bx) * ceil(ny/by) * nz
+ * with bx = nx rounded up to a multiple of 32 (at most 256) and by = 256/bx
+ * (8,388,608 cells when nx is a multiple of 256, fewer otherwise), and
+ * 32,768 tabulated inflow-profile values (one per cell of each parabolic
+ * velocity boundary); larger requests return LBM_ERR_ARG before any device
+ * call.  Boundaries with LBM_PROFILE_TABLE are refused (LBM_ERR_SUP): their
+ * tables live in a handle.  With parabolic velocity boundaries the call
+ * copies their profile to the scratch and waits for `stream` before it
+ * returns.  Every call shares that array, so calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialised by the caller.
+ * The first call on each device looks up the array's device address and
+ * keeps it for the life of the process; make that call before any stream
+ * capture.  A cudaDeviceReset() invalidates the kept address (as it does
+ * every handle): do not call this entry point after resetting a device.
  * Errors are reported through lbm_last_error(NULL). */
 int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f_dev,
                           const void* gamma_dev, double* J_dev, void* stream);

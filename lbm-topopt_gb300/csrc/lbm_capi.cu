@@ -32,9 +32,15 @@ int64_t bc_npos(const lbm_bc& b) {
   return (int64_t)(b.box[3] - b.box[2] + 1) * (b.box[5] - b.box[4] + 1);
 }
 
-double bc_time_factor(const lbm_bc& b, int t) {
+double bc_time_factor(const lbm_bc& b, int t, int t_start) {
   if (b.time_law == LBM_TIME_SINE)
     return b.amp == 0. ? 0. : b.amp * sin(2. * M_PI * (double)t / b.period);
+  if (b.time_law == LBM_TIME_RAMP) {
+    // StageTemp (applications/Regenerator2d/regenerator2d.cc:53-69)
+    if (t_start == INT_MAX || t <= t_start) return b.amp;
+    const long long s = (long long)t - t_start;
+    return b.amp + ((double)s < b.period ? sin(M_PI * (double)s / (2. * b.period)) : 1.);
+  }
   return (b.amp == 0.) ? 1. : 1. + b.amp * sin(2. * M_PI * (double)t / b.period);
 }
 
@@ -58,8 +64,8 @@ void bc_parabola(const lbm_config& c, const lbm_bc& b, double* out) {
     }
 }
 
-void fill_devbc(const lbm_bc& b, int t, int ncomp, const double* tab_d, const float* tab_f,
-                DevBC& d) {
+void fill_devbc(const lbm_bc& b, int t, int t_start, int ncomp, const double* tab_d,
+                const float* tab_f, DevBC& d) {
   d.kind = b.kind;
   d.face = b.face;
   d.profile = b.profile;
@@ -68,7 +74,7 @@ void fill_devbc(const lbm_bc& b, int t, int ncomp, const double* tab_d, const fl
   d.n_t = d.tang_x ? b.box[1] - b.box[0] + 1 : b.box[3] - b.box[2] + 1;
   d.ncomp = tab_d ? ncomp : 0;
   // value(t) = value * T(t), evaluated here once per launch
-  d.value = b.value * bc_time_factor(b, t);
+  d.value = b.value * bc_time_factor(b, t, t_start);
   d.value_f = (float)d.value;
   d.vshift = d.value - 1.;
   d.vshift_f = (float)d.vshift;
@@ -169,6 +175,12 @@ struct lbm_handle {
   int tab_nt[LBM_MAX_BC] = {};
   int tab_ncomp[LBM_MAX_BC] = {};
   int64_t table_gen = 0;   // bumped when a table moves to a new device buffer
+  // first step whose state's objective counts (a steady phase before it adds none)
+  int obj_from = 1;
+  // step at which the last steady phase ended (start of LBM_TIME_RAMP ramps)
+  int t_phase = INT_MAX;
+  // 1/D of the regenerator efficiency, D = sum (1-gamma)(Tb - Ti) over obj_out
+  double regen_invD = 0.;
   int t = 0;
   bool have_design = false, have_state = false, have_adjoint = false;
   bool accumulate = false;   // objective sums over steps into the warp partials
@@ -246,6 +258,22 @@ void launch_max_change(size_t pop_bytes, const void* a, const void* b, int Q, lo
     k_max_change<float><<<blocks, 256, 0, st>>>((const float*)a, (const float*)b, Q, P, ncell, bits);
   else
     k_max_change<__half><<<blocks, 256, 0, st>>>((const __half*)a, (const __half*)b, Q, P, ncell, bits);
+}
+
+// sens[c] += coef * (*J) over the cells of box b (x fastest): the design
+// term every box cell shares (the regenerator efficiency's 1/D derivative).
+__global__ void k_box_add_scaled(double* __restrict__ sens, int nx, int ny, int x0, int x1, int y0,
+                                 int y1, int z0, int z1, const double* __restrict__ J, double coef) {
+  const int bx = x1 - x0 + 1, by = y1 - y0 + 1;
+  const long long n = (long long)bx * by * (z1 - z0 + 1);
+  const double v = coef * (*J);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = x0 + (int)(i % bx);
+    const int y = y0 + (int)((i / bx) % by);
+    const int z = z0 + (int)(i / ((long long)bx * by));
+    sens[((long long)z * ny + y) * nx + x] += v;
+  }
 }
 
 size_t state_bytes(const lbm_handle* h) { return (size_t)h->Q * h->P * h->pop_bytes; }
@@ -345,8 +373,11 @@ int validate(const lbm_config& c) {
     if (b.profile != LBM_PROFILE_UNIFORM && b.profile != LBM_PROFILE_PARABOLIC &&
         b.profile != LBM_PROFILE_TABLE)
       return fail(nullptr, LBM_ERR_ARG, "boundary %d: unknown profile %d", k, b.profile);
-    if (b.time_law != LBM_TIME_OFFSET_SINE && b.time_law != LBM_TIME_SINE)
+    if (b.time_law != LBM_TIME_OFFSET_SINE && b.time_law != LBM_TIME_SINE &&
+        b.time_law != LBM_TIME_RAMP)
       return fail(nullptr, LBM_ERR_ARG, "boundary %d: unknown time law %d", k, b.time_law);
+    if (b.time_law == LBM_TIME_RAMP && !(b.period > 0.))
+      return fail(nullptr, LBM_ERR_ARG, "boundary %d: a ramp needs period > 0", k);
     if (b.amp != 0. && !(b.period > 0.))
       return fail(nullptr, LBM_ERR_ARG, "boundary %d: oscillation needs period > 0", k);
     if (!std::isfinite(b.value) || !std::isfinite(b.amp))
@@ -354,6 +385,11 @@ int validate(const lbm_config& c) {
     for (int a = 0; a < 3; ++a)
       if (!std::isfinite(b.dir[a])) return fail(nullptr, LBM_ERR_ARG, "boundary %d: bad direction", k);
   }
+  for (int i = 0; i < 4; ++i)
+    if (!std::isfinite(c.obj_param[i]))
+      return fail(nullptr, LBM_ERR_ARG, "objective parameter %d is not finite", i);
+  if (c.objective == LBM_OBJ_REGENERATOR_EFFICIENCY && c.obj_param[1] == c.obj_param[0])
+    return fail(nullptr, LBM_ERR_ARG, "regenerator efficiency needs Tb != Ti (obj_param[1], [0])");
   if (c.objective != LBM_OBJ_NONE) {
     ObjectiveInfo oi;
     if (!objective_info(c.objective, &oi))
@@ -433,7 +469,7 @@ KParams base_params(const lbm_handle* h, int t) {
     const int64_t row = h->tab_nt[k] > 0 ? (int64_t)(t % h->tab_nt[k]) * bc_npos(b) *
                                                (h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1)
                                          : 0;
-    fill_devbc(b, t, h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1,
+    fill_devbc(b, t, h->t_phase, h->tab_ncomp[k] > 0 ? h->tab_ncomp[k] : 1,
                h->bcprof_d[k] ? h->bcprof_d[k] + row : nullptr,
                h->bcprof_f[k] ? h->bcprof_f[k] + row : nullptr, p.bc[k]);
     if (bc_on_y_face(b)) p.bc_y = 1;
@@ -462,6 +498,8 @@ KParams base_params(const lbm_handle* h, int t) {
     double nu = (1. / c.omega - 0.5) / 3.;
     md.cv_diss = 4.5 * nu * c.omega * c.omega;
   }
+  md.obj_p[0] = c.obj_param[0];
+  md.obj_p[1] = c.objective == LBM_OBJ_REGENERATOR_EFFICIENCY ? c.obj_weight * h->regen_invD : 0.;
   ModelParams<float>& mf = p.mf;
   mf.omega = (float)md.omega;
   for (int i = 0; i < 8; ++i) mf.mrt[i] = (float)md.mrt[i];
@@ -476,6 +514,8 @@ KParams base_params(const lbm_handle* h, int t) {
   mf.w_in = (float)md.w_in;
   mf.w_out = (float)md.w_out;
   mf.cv_diss = (float)md.cv_diss;
+  mf.obj_p[0] = (float)md.obj_p[0];
+  mf.obj_p[1] = (float)md.obj_p[1];
   p.partial = h->partial;
   p.counter = h->counter;
   p.accumulate = h->accumulate ? 1 : 0;
@@ -584,7 +624,7 @@ int adjoint_at(lbm_handle* h, const void* f) {
   p.fin = f;
   p.lam_in = h->lam[h->lcur];
   p.lam_out = h->lam[1 - h->lcur];
-  p.eval_obj = (h->t >= 1 && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
+  p.eval_obj = (h->t >= h->obj_from && h->cfg.objective != LBM_OBJ_NONE) ? 1 : 0;
   int rc = launch(h, h->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, p, nullptr);
   if (rc) return rc;
   h->lcur ^= 1;
@@ -617,6 +657,37 @@ int init_into(lbm_handle* h, void* out) {
 }
 
 int init_state(lbm_handle* h) { return init_into(h, h->f[h->cur]); }
+
+// D = sum over obj_out of (1 - gamma)(Tb - Ti) of the regenerator efficiency,
+// from the design on the host.
+void set_regen_denominator(lbm_handle* h, const double* gamma) {
+  const lbm_config& c = h->cfg;
+  if (c.objective != LBM_OBJ_REGENERATOR_EFFICIENCY) return;
+  const int* b = c.obj_out;
+  double d = 0.;
+  for (int z = b[4]; z <= b[5]; ++z)
+    for (int y = b[2]; y <= b[3]; ++y)
+      for (int x = b[0]; x <= b[1]; ++x)
+        d += (1. - gamma[((int64_t)z * c.ny + y) * c.nx + x]) * (c.obj_param[1] - c.obj_param[0]);
+  h->regen_invD = 1. / d;   // no solid in the box: inf, and the objective is reported non-finite
+}
+
+// The objective's design term shared by every box cell, from the objective
+// value *J (device): the regenerator efficiency's d(1/D)/dgamma part,
+// J (Tb - Ti) / D.  Nothing for the other objectives.
+int add_design_term(lbm_handle* h, const double* J) {
+  const lbm_config& c = h->cfg;
+  if (c.objective != LBM_OBJ_REGENERATOR_EFFICIENCY) return 0;
+  const int* b = c.obj_out;
+  const double coef = (c.obj_param[1] - c.obj_param[0]) * h->regen_invD;
+  const long long n = (long long)(b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1);
+  const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 1024);
+  k_box_add_scaled<<<blocks, 256, 0, h->stream>>>(h->sens, c.nx, c.ny, b[0], b[1], b[2], b[3], b[4],
+                                                  b[5], J, coef);
+  h->launches++;
+  CUDA_OR_FAIL(h, cudaGetLastError());
+  return 0;
+}
 
 }  // namespace
 
@@ -852,6 +923,7 @@ int lbm_set_design(lbm_handle* h, const double* gamma) {
   }
   int rc = ensure_stage(h);
   if (rc) return rc;
+  set_regen_denominator(h, gamma);
   CUDA_OR_FAIL(h, cudaMemcpyAsync(h->stage, gamma, (size_t)h->ncell * sizeof(double),
                                   cudaMemcpyHostToDevice, h->stream));
   KParams p = base_params(h, 0);
@@ -868,6 +940,11 @@ int lbm_set_design_device(lbm_handle* h, const double* gamma_dev) {
   if (!gamma_dev) return fail(h, LBM_ERR_ARG, "null design pointer");
   // the caller's producing work must be complete before this stream reads it
   CUDA_OR_FAIL(h, cudaDeviceSynchronize());
+  if (h->cfg.objective == LBM_OBJ_REGENERATOR_EFFICIENCY) {
+    std::vector<double> g((size_t)h->ncell);
+    CUDA_OR_FAIL(h, cudaMemcpy(g.data(), gamma_dev, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    set_regen_denominator(h, g.data());
+  }
   KParams p = base_params(h, 0);
   int rc = launch(h, K_GAMMA, p, const_cast<double*>(gamma_dev));
   if (rc) return rc;
@@ -896,6 +973,8 @@ int lbm_init_equilibrium(lbm_handle* h, const double* macros) {
     cudaFree(h->init_mac);
     h->init_mac = nullptr;
   }
+  h->t_phase = INT_MAX;   // a new run: no steady phase yet
+  h->obj_from = 1;
   int rc = init_state(h);
   if (rc) return rc;
   return sync(h);
@@ -933,6 +1012,7 @@ int lbm_forward_steady(lbm_handle* h, int max_steps, int check_every, double tol
     }
   }
   if ((rc = sync(h))) return rc;
+  h->t_phase = h->t;   // LBM_TIME_RAMP boundaries start from here
   if (steps) *steps = k;
   if (change) *change = last;
   return LBM_OK;
@@ -1051,7 +1131,14 @@ int lbm_adjoint_step(lbm_handle* h) {
   if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
   if (!h->have_design || !h->have_state) return fail(h, LBM_ERR_STATE, "no design or state");
   if (!h->have_adjoint) return fail(h, LBM_ERR_STATE, "adjoint not reset (lbm_adjoint_reset)");
-  int rc = adjoint_step(h);
+  int rc;
+  if (h->cfg.objective == LBM_OBJ_REGENERATOR_EFFICIENCY && h->t >= h->obj_from) {
+    // this step's share of the 1/D design term needs the step's objective
+    if ((rc = ensure_jcap(h, 1))) return rc;
+    if ((rc = objective_only(h, h->jdev))) return rc;
+    if ((rc = add_design_term(h, h->jdev))) return rc;
+  }
+  rc = adjoint_step(h);
   if (rc) return rc;
   return sync(h);
 }
@@ -1085,14 +1172,25 @@ int lbm_gradient(lbm_handle* h, int nsteps, int nsnap, double* J, double* dJdgam
   return lbm_gradient_schedule(h, nsteps, nsnap, LBM_SCHEDULE_DYNAMIC, J, dJdgamma, stats);
 }
 
-int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, double* J,
-                          double* dJdgamma, lbm_gradient_stats* stats) {
-  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
-  if (nsteps < 1) return fail(h, LBM_ERR_ARG, "nsteps %d < 1", nsteps);
-  if (nsnap < 2) return fail(h, LBM_ERR_ARG, "nsnapshots %d < 2", nsnap);
-  if (schedule != LBM_SCHEDULE_DYNAMIC && schedule != LBM_SCHEDULE_STATIC)
-    return fail(h, LBM_ERR_ARG, "unknown checkpoint schedule %d", schedule);
-  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+}  // extern "C"
+
+namespace {
+
+// The steady phase of a regenerator-style gradient: run until the largest
+// one-step change of any population, measured every check_every steps, is
+// below tol (or max_steps steps).
+struct SteadyPhase {
+  int max_steps, check_every;
+  double tol;
+  int steps = 0;        // taken
+  double change = -1.;  // last measured
+};
+
+// The checkpointed forward sweep, reverse sweep and t = 0 term of
+// lbm_gradient_schedule and lbm_gradient_steady.  With `sp`, a steady phase
+// without objective comes first and nsteps objective steps follow it.
+int gradient_run(lbm_handle* h, int nsteps, int nsnap, int schedule, SteadyPhase* sp, double* J,
+                 double* dJdgamma, lbm_gradient_stats* stats) {
   int rc;
   // snapshot slots in device memory
   if ((int)h->slots.size() != nsnap) {
@@ -1110,7 +1208,7 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
       }
     }
   }
-  if ((rc = ensure_jcap(h, (size_t)nsteps))) return rc;
+  if ((rc = ensure_jcap(h, (size_t)nsteps + 1))) return rc;
   const bool obj = h->cfg.objective != LBM_OBJ_NONE;
   const size_t sb = state_bytes(h);
   WangSchedule ws(nsnap);
@@ -1145,20 +1243,51 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
   };
   act.save = save;
 
+  h->t_phase = INT_MAX;   // a new run: ramps wait for the steady phase
+  h->obj_from = 1;
   cudaEventRecord(h->ev[0], h->stream);
   {
     const int out = pool.scratch();
     if ((rc = init_into(h, pool_buffer(h, out)))) return rc;
     pool.set_current(out);
   }
-  // J = sum_t F(f_t), summed in the warp partials across the sweep
-  if (obj && (rc = begin_accumulate(h))) return rc;
-  if ((rc = save(place(0)))) {
-    h->accumulate = false;
-    return rc;
+  if ((rc = save(place(0)))) return rc;
+  int steady = 0;
+  if (sp) {
+    // regenerator2d.cc:282-310: no objective; the states are checkpointed too
+    // (the reverse sweep runs through them with an empty objective)
+    unsigned long long* bits = (unsigned long long*)(h->jdev + nsteps);
+    while (steady < sp->max_steps) {
+      const int prev = pool.current();
+      if ((rc = advance(nullptr))) return rc;
+      ++steady;
+      if ((rc = save(place(steady)))) return rc;
+      if (steady % sp->check_every == 0 || steady == sp->max_steps) {
+        // the step's input is still intact in its buffer (the next step writes later)
+        CUDA_OR_FAIL(h, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), h->stream));
+        const long long total = (long long)h->Q * h->ncell;
+        const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 4096);
+        launch_max_change(h->pop_bytes, cur_buf(), pool_buffer(h, prev), h->Q, h->P, h->ncell,
+                          bits, blocks, h->stream);
+        CUDA_OR_FAIL(h, cudaGetLastError());
+        unsigned long long hb = 0;
+        CUDA_OR_FAIL(h, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(h, cudaStreamSynchronize(h->stream));
+        memcpy(&sp->change, &hb, sizeof(double));
+        if (!std::isfinite(sp->change))
+          return fail(h, LBM_ERR_NONFINITE, "state is not finite at step %d", h->t);
+        if (sp->change < sp->tol) break;
+      }
+    }
+    sp->steps = steady;
+    h->t_phase = steady;      // StageTemp: the ramp starts after the steady phase
+    h->obj_from = steady + 1; // the objective counts the states after it
   }
-  for (int s = 0; s < nsteps; ++s) {
-    if ((rc = advance((obj && s >= 1) ? h->jdev : nullptr))) break;
+  // J = sum_t F(f_t) over t = obj_from .. steady + nsteps, summed in the warp
+  // partials across the sweep
+  if (obj && (rc = begin_accumulate(h))) return rc;
+  for (int s = steady; s < steady + nsteps; ++s) {
+    if ((rc = advance((obj && s >= h->obj_from) ? h->jdev : nullptr))) break;
     if ((rc = save(place(s + 1)))) break;
   }
   if (!rc && obj && !(rc = objective_at(h, cur_buf(), h->jdev))) rc = end_accumulate(h, h->jdev);
@@ -1167,7 +1296,8 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
   cudaEventRecord(h->ev[1], h->stream);
   if ((rc = zero_adjoint(h))) return rc;
   h->have_adjoint = true;
-  for (int s = nsteps; s >= 1; --s) {
+  const int total = steady + nsteps;
+  for (int s = total; s >= 1; --s) {
     try {
       rc = ws.get_forward_solution(s, act);
     } catch (const std::exception& ex) {
@@ -1183,6 +1313,8 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
   h->cur = 0;
   if ((rc = init_state(h))) return rc;
   if ((rc = adjoint_step(h))) return rc;
+  // the objective's design term shared by the box cells, from J
+  if (obj && (rc = add_design_term(h, h->jdev))) return rc;
   cudaEventRecord(h->ev[2], h->stream);
   if ((rc = sync(h))) return rc;
   double acc = 0.;
@@ -1198,13 +1330,44 @@ int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, do
     float a = 0.f, b = 0.f;
     cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
     cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
-    stats->forward_steps = nsteps;
+    stats->forward_steps = total;
     stats->recomputed_steps = ws.recomputed();
-    stats->adjoint_steps = nsteps;
+    stats->adjoint_steps = total;
     stats->forward_ms = a;
     stats->reverse_ms = b;
   }
   return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_gradient_schedule(lbm_handle* h, int nsteps, int nsnap, int schedule, double* J,
+                          double* dJdgamma, lbm_gradient_stats* stats) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (nsteps < 1) return fail(h, LBM_ERR_ARG, "nsteps %d < 1", nsteps);
+  if (nsnap < 2) return fail(h, LBM_ERR_ARG, "nsnapshots %d < 2", nsnap);
+  if (schedule != LBM_SCHEDULE_DYNAMIC && schedule != LBM_SCHEDULE_STATIC)
+    return fail(h, LBM_ERR_ARG, "unknown checkpoint schedule %d", schedule);
+  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+  return gradient_run(h, nsteps, nsnap, schedule, nullptr, J, dJdgamma, stats);
+}
+
+int lbm_gradient_steady(lbm_handle* h, int max_steady, int check_every, double tol,
+                        int n_unsteady, int nsnap, int* steady_steps, double* J, double* dJdgamma,
+                        lbm_gradient_stats* stats) {
+  if (!h) return fail(nullptr, LBM_ERR_ARG, "null handle");
+  if (max_steady < 1 || check_every < 1)
+    return fail(h, LBM_ERR_ARG, "need max_steady >= 1 and check_every >= 1");
+  if (!(tol >= 0.)) return fail(h, LBM_ERR_ARG, "tol must be >= 0");
+  if (n_unsteady < 1) return fail(h, LBM_ERR_ARG, "n_unsteady %d < 1", n_unsteady);
+  if (nsnap < 2) return fail(h, LBM_ERR_ARG, "nsnapshots %d < 2", nsnap);
+  if (!h->have_design) return fail(h, LBM_ERR_STATE, "no design set (lbm_set_design)");
+  SteadyPhase sp{max_steady, check_every, tol};
+  int rc = gradient_run(h, n_unsteady, nsnap, LBM_SCHEDULE_DYNAMIC, &sp, J, dJdgamma, stats);
+  if (steady_steps) *steady_steps = sp.steps;
+  return rc;
 }
 
 int lbm_time_steps(lbm_handle* h, int which, int nsteps, float* ms) {
@@ -1741,6 +1904,10 @@ int lbm_batch_create(const lbm_config* cfgs, int n, lbm_batch** out) {
     if (cfgs[i].lattice != cfgs[0].lattice || cfgs[i].collision != cfgs[0].collision ||
         cfgs[i].storage != cfgs[0].storage)
       return bfail(nullptr, LBM_ERR_SUP, "batched lattices must share lattice, collision and storage");
+  for (int i = 0; i < n; ++i)
+    if (cfgs[i].objective == LBM_OBJ_REGENERATOR_EFFICIENCY)
+      return bfail(nullptr, LBM_ERR_SUP,
+                   "lattice %d: the regenerator efficiency runs on single handles only", i);
   lbm_batch* b = new (std::nothrow) lbm_batch();
   if (!b) return bfail(nullptr, LBM_ERR_MEM, "host allocation failed");
   for (int i = 0; i < n; ++i) {

@@ -246,6 +246,7 @@ struct ModelParams {
   C diff, ramp_q, ramp_ck, heat_rate, heat_T;
   C obj_weight, w_in, w_out;   // w_in = inv_in*obj_weight, w_out = inv_out*obj_weight
   C cv_diss;                   // (9/2) nu omega^2 of the dissipation objective
+  C obj_p[2];                  // objective parameters (regenerator efficiency: Ti, w/D)
 };
 
 struct KParams {

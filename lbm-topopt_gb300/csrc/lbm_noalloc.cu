@@ -11,6 +11,7 @@
 // the library keeps until the process exits.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -24,8 +25,9 @@ using namespace lbm;
 
 namespace {
 
-// Scratch limits: at most kMaxBlocks 256-thread blocks (8,388,608 cells) and
-// kMaxProfile tabulated inflow-profile entries over all velocity boundaries.
+// Scratch limits: at most kMaxBlocks 256-thread blocks (8,388,608 cells when
+// nx is a multiple of 256; the launch pads each row of blocks) and kMaxProfile
+// tabulated inflow-profile entries over all parabolic velocity boundaries.
 constexpr int kMaxBlocks = 32768;
 constexpr int kMaxProfile = 32768;
 constexpr size_t kCounterBytes = 256;
@@ -39,6 +41,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
+// Device address of the array per device, looked up by the first call on that
+// device.  A cudaDeviceReset() of the device would leave a stale address here
+// (the array gets a new one in the new context); the library is not used
+// across device resets.
 void* g_scratch_ptr[kMaxDevices] = {};
 // host-side staging of the profile tables (static storage: no heap allocation)
 double g_prof_d[kMaxProfile];
@@ -83,7 +89,7 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
   if (nblocks > kMaxBlocks)
     return fail(LBM_ERR_ARG, "lattice needs " + std::to_string(nblocks) +
                                  " thread blocks; the allocation-free path holds scratch for " +
-                                 std::to_string(kMaxBlocks) + " (at most 8,388,608 cells)");
+                                 std::to_string(kMaxBlocks));
   long long nprof = 0;
   for (int k = 0; k < c.nbc; ++k) {
     const lbm_bc& b = c.bc[k];
@@ -91,8 +97,14 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
       return fail(LBM_ERR_SUP, "boundary " + std::to_string(k) +
                                    ": tabulated profiles live in a handle; the allocation-free "
                                    "path takes uniform and parabolic profiles only");
+    if (b.time_law == LBM_TIME_RAMP)
+      return fail(LBM_ERR_SUP, "boundary " + std::to_string(k) +
+                                   ": ramps start after a handle's steady phase; the allocation-"
+                                   "free path has none");
     if (parabolic(b)) nprof += bc_npos(b);
   }
+  if (c.objective == LBM_OBJ_REGENERATOR_EFFICIENCY)
+    return fail(LBM_ERR_SUP, "the regenerator efficiency's denominator comes from a handle's design");
   if (nprof > kMaxProfile)
     return fail(LBM_ERR_ARG, "inflow profiles need " + std::to_string(nprof) +
                                  " entries; the allocation-free path holds " +
@@ -170,7 +182,8 @@ extern "C" int lbm_objective_noalloc(const lbm_config* cfg, int t, const void* f
       bc_parabola(c, b, g_prof_d + off);
       for (long long i = 0; i < bc_npos(b); ++i) g_prof_f[off + i] = (float)g_prof_d[off + i];
     }
-    fill_devbc(b, t, 1, par ? prof_d + off : nullptr, par ? prof_f + off : nullptr, p.bc[k]);
+    fill_devbc(b, t, INT_MAX, 1, par ? prof_d + off : nullptr, par ? prof_f + off : nullptr,
+               p.bc[k]);
     if (bc_on_y_face(b)) p.bc_y = 1;
     if (par) off += bc_npos(b);
   }

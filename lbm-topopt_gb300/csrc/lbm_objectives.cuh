@@ -278,12 +278,82 @@ struct ObjDissipation {
   }
 };
 
+// DomainTemperature2d (functionals/domainTemperature2d.hh:13-40): w (mean T
+// over the box).
+struct ObjDomainTemperature {
+  static constexpr int id = LBM_OBJ_DOMAIN_TEMPERATURE;
+  static constexpr unsigned uses = kUsesOut;
+  static constexpr bool thermal = true;
+  template <int LAT, bool SHIFT, class C>
+  static __device__ __forceinline__ C evaluate(const C* f, C, int x, int y, int z,
+                                               const KParams& p) {
+    if constexpr (LAT != LAT_D2Q9_D2Q5) {
+      return C(0.);
+    } else {
+      if (!in_box(p.obj_out, x, y, z)) return C(0.);
+      return mp<C>(p).w_out * (f[9] + f[10] + f[11] + f[12] + f[13]);
+    }
+  }
+  template <int LAT, bool SHIFT, class C>
+  static __device__ __forceinline__ void source(const C*, C, C* lam, C&, int x, int y, int z,
+                                                const KParams& p) {
+    if constexpr (LAT == LAT_D2Q9_D2Q5) {
+      if (in_box(p.obj_out, x, y, z)) {
+        const C v = mp<C>(p).w_out;
+#pragma unroll
+        for (int d = 9; d < 14; ++d) lam[d] += v;
+      }
+    }
+  }
+};
+
+// RegeneratorEfficiency2d (functionals/regeneratorEfficiency2d.hh:16-88):
+// J_t = w sum (1-gamma)(T - Ti) / D over the box, D = sum (1-gamma)(Tb - Ti)
+// (design-dependent, computed by the host when the design is set; obj_p[1] =
+// w/D).  The per-cell parts are here; the derivative of 1/D (dD/dgamma_c =
+// -(Tb - Ti) in the box) gives every box cell the same term J (Tb - Ti)/D,
+// which the host adds once per reverse sweep (or per reverse step) from J.
+// The reference's adjoint sources use timeConst where the evaluate uses
+// none and vice versa (adjointCollideSource divides by timeConst * D,
+// adjointSensitivitySource leaves timeConst off the -(T - Ti) D term); they
+// equal these derivatives only for timeConst = 1.
+struct ObjRegeneratorEfficiency {
+  static constexpr int id = LBM_OBJ_REGENERATOR_EFFICIENCY;
+  static constexpr unsigned uses = kUsesOut;
+  static constexpr bool thermal = true;
+  template <int LAT, bool SHIFT, class C>
+  static __device__ __forceinline__ C evaluate(const C* f, C g, int x, int y, int z,
+                                               const KParams& p) {
+    if constexpr (LAT != LAT_D2Q9_D2Q5) {
+      return C(0.);
+    } else {
+      if (!in_box(p.obj_out, x, y, z)) return C(0.);
+      const C T = f[9] + f[10] + f[11] + f[12] + f[13];
+      return mp<C>(p).obj_p[1] * ((C(1.) - g) * (T - mp<C>(p).obj_p[0]));
+    }
+  }
+  template <int LAT, bool SHIFT, class C>
+  static __device__ __forceinline__ void source(const C* f, C g, C* lam, C& dg, int x, int y,
+                                                int z, const KParams& p) {
+    if constexpr (LAT == LAT_D2Q9_D2Q5) {
+      if (in_box(p.obj_out, x, y, z)) {
+        const C wd = mp<C>(p).obj_p[1];
+        const C v = wd * (C(1.) - g);
+#pragma unroll
+        for (int d = 9; d < 14; ++d) lam[d] += v;
+        const C T = f[9] + f[10] + f[11] + f[12] + f[13];
+        dg -= wd * (T - mp<C>(p).obj_p[0]);
+      }
+    }
+  }
+};
+
 template <class... Os>
 struct ObjList {};
 
 // Every objective the kernels know.  Append a functor here to add one.
-using ObjectiveList =
-    ObjList<ObjPressureDrop, ObjDissipation, ObjHeatFlux, ObjOutflow, ObjThroughFlow>;
+using ObjectiveList = ObjList<ObjPressureDrop, ObjDissipation, ObjHeatFlux, ObjOutflow,
+                              ObjThroughFlow, ObjDomainTemperature, ObjRegeneratorEfficiency>;
 
 // Host-side facts about an objective (validation, box normalisation).
 struct ObjectiveInfo {

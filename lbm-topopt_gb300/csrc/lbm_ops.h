@@ -55,14 +55,14 @@ int validate_config(const lbm_config& c);
 int64_t bc_npos(const lbm_bc& b);
 // Whether b lies on a south or north face.
 bool bc_on_y_face(const lbm_bc& b);
-// T(t) of b's time law.
-double bc_time_factor(const lbm_bc& b, int t);
+// T(t) of b's time law; t_start: where LBM_TIME_RAMP ramps begin (INT_MAX: not yet).
+double bc_time_factor(const lbm_bc& b, int t, int t_start);
 // Parabolic factors of a velocity boundary over its box, bc_npos(b) values.
 void bc_parabola(const lbm_config& c, const lbm_bc& b, double* out);
 // Device parameters of boundary b at time step t.  tab_d / tab_f: the factor
 // (ncomp = 1) or velocity (ncomp = 2, 3) table row of step t, or null.
-void fill_devbc(const lbm_bc& b, int t, int ncomp, const double* tab_d, const float* tab_f,
-                DevBC& d);
+void fill_devbc(const lbm_bc& b, int t, int t_start, int ncomp, const double* tab_d,
+                const float* tab_f, DevBC& d);
 
 // The facts of objective `id` from the kernels' objective list; false if unknown.
 bool objective_info(int id, ObjectiveInfo* out);

@@ -38,9 +38,9 @@ BC_VELOCITY, BC_PRESSURE, BC_TEMPERATURE = 1, 2, 3
 BC_VELOCITY_STANDARD, BC_PRESSURE_STANDARD = 4, 5
 FACE_WEST, FACE_EAST, FACE_SOUTH, FACE_NORTH = 0, 1, 2, 3
 PROFILE_UNIFORM, PROFILE_PARABOLIC, PROFILE_TABLE = 0, 1, 2
-TIME_OFFSET_SINE, TIME_SINE = 0, 1
+TIME_OFFSET_SINE, TIME_SINE, TIME_RAMP = 0, 1, 2
 OBJ_NONE, OBJ_PRESSURE_DROP, OBJ_DISSIPATION, OBJ_HEAT_FLUX, OBJ_OUTFLOW = 0, 1, 2, 3, 4
-OBJ_THROUGH_FLOW = 5
+OBJ_THROUGH_FLOW, OBJ_DOMAIN_TEMPERATURE, OBJ_REGENERATOR_EFFICIENCY = 5, 6, 7
 SCHEDULE_DYNAMIC, SCHEDULE_STATIC = 0, 1
 MAX_BC = 8
 
@@ -70,7 +70,7 @@ class CConfig(C.Structure):
                 ("heat_rate", C.c_double), ("heat_T", C.c_double),
                 ("nbc", C.c_int), ("bc", CBC * MAX_BC),
                 ("objective", C.c_int), ("obj_in", C.c_int * 6), ("obj_out", C.c_int * 6),
-                ("obj_weight", C.c_double)]
+                ("obj_weight", C.c_double), ("obj_param", C.c_double * 4)]
 
 
 class CGradStats(C.Structure):
@@ -118,6 +118,7 @@ class Config:
     obj_in: Sequence[int] = (0, 0, 0, 0, 0, 0)
     obj_out: Sequence[int] = (0, 0, 0, 0, 0, 0)
     obj_weight: float = 1.0
+    obj_param: Sequence[float] = (0.0, 0.0, 0.0, 0.0)
 
     @property
     def ncells(self) -> int:
@@ -164,6 +165,8 @@ class Config:
             c.obj_in[i] = int(self.obj_in[i])
             c.obj_out[i] = int(self.obj_out[i])
         c.obj_weight = self.obj_weight
+        for i, v in enumerate(list(self.obj_param)[:4]):
+            c.obj_param[i] = float(v)
         return c
 
 
@@ -231,6 +234,8 @@ def load_library(path: Optional[str] = None) -> C.CDLL:
         "lbm_batch_get_reverse_variant": (C.c_int, [H]),
         "lbm_forward_steady": (C.c_int, [H, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int),
                                          C.POINTER(C.c_double)]),
+        "lbm_gradient_steady": (C.c_int, [H, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                          C.POINTER(C.c_int), dp, dp, C.POINTER(CGradStats)]),
         "lbm_get_dims": (C.c_int, [H, C.POINTER(C.c_int)]),
         "lbm_write_petsc_vec": (C.c_int, [C.c_char_p, dp, C.c_int64]),
         "lbm_read_petsc_vec": (C.c_int, [C.c_char_p, dp, C.c_int64, C.POINTER(C.c_int64)]),
@@ -449,6 +454,18 @@ class Handle:
         self._check(self.lib.lbm_gradient_schedule(self.h, int(nsteps), int(nsnapshots),
                                                    int(schedule), _ptr(J), _ptr(s), C.byref(st)))
         return float(J[0]), s, st
+
+    def gradient_steady(self, max_steady: int, check_every: int, tol: float, n_unsteady: int,
+                        nsnapshots: int):
+        """lbm_gradient_steady: (J, dJ/dgamma, stats, steady steps)."""
+        J = np.zeros(1)
+        s = np.empty(self.cfg.ncells)
+        st = CGradStats()
+        S = C.c_int()
+        self._check(self.lib.lbm_gradient_steady(self.h, int(max_steady), int(check_every),
+                                                 float(tol), int(n_unsteady), int(nsnapshots),
+                                                 C.byref(S), _ptr(J), _ptr(s), C.byref(st)))
+        return float(J[0]), s, st, S.value
 
     def time_steps(self, which: int, nsteps: int) -> float:
         ms = C.c_float()

@@ -20,8 +20,9 @@ import numpy as np
 
 from lbmgpu import (BC_PRESSURE, BC_TEMPERATURE, BC_VELOCITY, BGK, D2Q9, D2Q9_D2Q5, D3Q19,
                     FACE_EAST, FACE_NORTH, FACE_WEST, MRT, OBJ_DISSIPATION, OBJ_HEAT_FLUX,
-                    OBJ_PRESSURE_DROP, OBJ_THROUGH_FLOW, PROFILE_PARABOLIC, PROFILE_TABLE,
-                    STORE_FP64, TIME_SINE, Boundary, Config)
+                    OBJ_PRESSURE_DROP, OBJ_REGENERATOR_EFFICIENCY, OBJ_THROUGH_FLOW,
+                    PROFILE_PARABOLIC, PROFILE_TABLE, STORE_FP64, TIME_RAMP, TIME_SINE, Boundary,
+                    Config)
 
 SEED_BASE = 20261203
 MASK64 = (1 << 64) - 1
@@ -158,6 +159,55 @@ def pump_inflow_profile(cfg: Config) -> np.ndarray:
     mid, r = (n - 1) / 2.0, th / 2.0
     x = np.arange(th + 1, 2 * th + 1, dtype=np.float64)
     return ((r * r - (x - mid) * (x - mid)) / (r * r))[None, :]
+
+
+def regenerator_2d(nx: int, ny: int, *, velocity: float = 0.05, reynolds: float = 30.0,
+                   prandtl: float = 0.71, ck: float = 0.0025, delta_T: float = 2.0,
+                   ramp: float = 200.0, storage: int = STORE_FP64, n_unsteady: int = 2000,
+                   objective: int = OBJ_REGENERATOR_EFFICIENCY) -> Config:
+    """The regenerator's set-up (applications/Regenerator2d/regenerator2d.cc:346-436)
+    on the D2Q9 + D2Q5 lattice: parabolic Zou-He velocity inlet (u_max = velocity,
+    nu from Re on the channel height), Zou-He pressure outlet rho = 1, and a
+    Dirichlet inlet temperature that holds T0 = 0 through the steady phase and then
+    ramps to delta_T over `ramp` steps (StageTemp, regenerator2d.cc:53-69); the
+    solid conducts Ck times the fluid (RAMP q = 1, regenerator2d.cc:376-381) and
+    partial bounce-back uses the plain BP interpolation with q = 1
+    (regenerator2d.cc:364).  The objective measures the middle of the channel
+    (obj_out, x = nx/4 .. 3nx/4): by default the regenerator efficiency with
+    Ti = 0, Tb = delta_T (functionals/regeneratorEfficiency2d.hh), averaged over
+    the unsteady steps.  Differences from the reference: the D2Q5 temperature
+    lattice instead of D2Q4, BGK flow instead of MRT, and the pull stream's mid-way
+    bounce-back for the walls and the thermal outlet instead of on-grid bounce-back
+    and a Neumann outlet."""
+    nu = velocity * ny / reynolds
+    omega = 1.0 / (3.0 * nu + 0.5)
+    inlet = (0, 0, 1, ny - 2, 0, 0)
+    outlet = (nx - 1, nx - 1, 1, ny - 2, 0, 0)
+    region = (nx // 4, 3 * nx // 4, 0, ny - 1, 0, 0)
+    return Config(
+        lattice=D2Q9_D2Q5, collision=BGK, storage=storage, nx=nx, ny=ny, nz=1,
+        omega=omega, interp_scale=1.0, interp_q=1.0,
+        diffusivity=nu / prandtl, ramp_q=1.0, ramp_ck=ck, heat_rate=0.0, heat_T=0.0,
+        bcs=[Boundary(BC_VELOCITY, FACE_WEST, inlet, velocity, PROFILE_PARABOLIC),
+             Boundary(BC_PRESSURE, FACE_EAST, outlet, 1.0),
+             Boundary(BC_TEMPERATURE, FACE_WEST, inlet, delta_T, amp=0.0, period=ramp,
+                      time_law=TIME_RAMP)],
+        objective=objective, obj_in=inlet, obj_out=region, obj_weight=1.0 / n_unsteady,
+        obj_param=(0.0, delta_T, 0.0, 0.0))
+
+
+def regenerator_design(nx: int, ny: int, seed: int) -> np.ndarray:
+    """Fluid except seeded solid plates across the middle of the channel (the
+    reference's initial plates, regenerator2d.cc:462-470, with seeded widths),
+    box-filtered once."""
+    r = splitmix64_uniform(seed, 8)
+    g = np.ones((ny, nx))
+    for k in range(3):
+        x0 = int(nx * (0.3 + 0.15 * k + 0.05 * r[k]))
+        w = max(3, int(nx * (0.04 + 0.02 * r[3 + k])))
+        y0, y1 = (1, int(ny * 0.45)) if k % 2 == 0 else (int(ny * 0.55), ny - 2)
+        g[y0:y1, x0:x0 + w] = 0.0
+    return np.clip(box_filter(g), 0.0, 1.0).ravel()
 
 
 def thermal_design(nx: int, ny: int, seed: int) -> np.ndarray:

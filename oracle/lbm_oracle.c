@@ -189,7 +189,12 @@ typedef struct {
   int nmac;             /* macros per cell */
   int64_t ncell;
   int nx, ny, nz, dim;
+  int t_phase;          /* step at which the last steady phase ended (LBM_TIME_RAMP) */
+  int obj_from;         /* first step whose state's objective counts */
 } model_t;
+
+/* Phase of the runs that follow (orc_set_phase): INT_MAX / 1 = no steady phase. */
+static int g_phase_start = 2147483647, g_obj_from = 1;
 
 static int model_init(model_t* m, const lbm_config* cfg) {
   memset(m, 0, sizeof(*m));
@@ -222,6 +227,14 @@ static int model_init(model_t* m, const lbm_config* cfg) {
   if (m->dim == 2) m->nz = 1;
   m->Q = m->Qf + m->Qt;
   m->ncell = (int64_t)m->nx * m->ny * m->nz;
+  m->t_phase = g_phase_start;
+  m->obj_from = g_obj_from;
+  return 0;
+}
+
+int orc_set_phase(int t_phase, int obj_from) {
+  g_phase_start = t_phase;
+  g_obj_from = obj_from;
   return 0;
 }
 
@@ -726,9 +739,15 @@ static void adjoint_stream_all(const model_t* m, const double* src, double* dst)
 /* ------------------------------------------------------------------ */
 /* Boundary conditions */
 
-static double time_factor(const lbm_bc* b, int t) {
+static double time_factor(const model_t* m, const lbm_bc* b, int t) {
   if (b->time_law == LBM_TIME_SINE)
     return b->amp == 0. ? 0. : b->amp * sin(2. * M_PI * (double)t / b->period);
+  if (b->time_law == LBM_TIME_RAMP) {
+    /* StageTemp (applications/Regenerator2d/regenerator2d.cc:53-69) */
+    if (m->t_phase == 2147483647 || t <= m->t_phase) return b->amp;
+    double s = (double)t - (double)m->t_phase;
+    return b->amp + (s < b->period ? sin(M_PI * s / (2. * b->period)) : 1.);
+  }
   if (b->amp == 0.) return 1.;
   return 1. + b->amp * sin(2. * M_PI * (double)t / b->period);
 }
@@ -793,7 +812,7 @@ static const double* table_entry(const lbm_bc* b, int k, int t, int x, int y, in
 /* Scalar value (density, temperature) of boundary k at a cell. */
 static double bc_scalar(const model_t* m, int k, int t, int x, int y, int z) {
   const lbm_bc* b = &m->cfg.bc[k];
-  double v = b->value * time_factor(b, t);
+  double v = b->value * time_factor(m, b, t);
   const double* e = table_entry(b, k, t, x, y, z);
   if (e) v *= e[0];
   return v;
@@ -810,7 +829,7 @@ static void bc_velocity(const model_t* m, int k, int t, int x, int y, int z, dou
     u[2] = g_tab[k].ncomp == 3 ? e[2] : 0.;
     return;
   }
-  double v = b->value * time_factor(b, t);
+  double v = b->value * time_factor(m, b, t);
   v *= e ? e[0] : profile(m, b, x, y, z);
   int nodir = b->dir[0] == 0. && b->dir[1] == 0. && b->dir[2] == 0.;
   for (int a = 0; a < 3; ++a) u[a] = v * (nodir ? (a == 0 ? 1. : 0.) : b->dir[a]);
@@ -1226,6 +1245,31 @@ static double objective(const model_t* m, const double* F, const double* gamma) 
           of -= tc * invOut * mac[1];
         }
     return iif + of;
+  } else if (c->objective == LBM_OBJ_DOMAIN_TEMPERATURE) {
+    /* DomainTemperature2d::evaluate (functionals/domainTemperature2d.hh:13-27) */
+    double inv = (double)(1. / box_count(c->obj_out)), pv = 0.;
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          const double* f = F + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
+          pv += tc * inv * (f[9] + f[10] + f[11] + f[12] + f[13]);
+        }
+    return pv;
+  } else if (c->objective == LBM_OBJ_REGENERATOR_EFFICIENCY) {
+    /* RegeneratorEfficiency2d::evaluate (functionals/regeneratorEfficiency2d.hh:16-35) */
+    double Ti = c->obj_param[0], Tb = c->obj_param[1], pvn = 0., pvd = 0.;
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          int64_t k = ((int64_t)z * m->ny + y) * m->nx + x;
+          const double* f = F + k * Q;
+          double T = f[9] + f[10] + f[11] + f[12] + f[13];
+          pvn += tc * (1. - gamma[k]) * (T - Ti);
+          pvd += (1. - gamma[k]) * (Tb - Ti);
+        }
+    return pvn / pvd;
   } else if (c->objective == LBM_OBJ_HEAT_FLUX) {
     double pout = 0.;
     const int* b = c->obj_out;
@@ -1298,6 +1342,44 @@ static void objective_source(const model_t* m, const double* F, const double* ga
         for (int x = b[0]; x <= b[1]; ++x) {
           double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
           for (int d = 0; d < m->Qf; ++d) a[d] -= invOut * tc * m->L->ex[d];
+        }
+  } else if (c->objective == LBM_OBJ_DOMAIN_TEMPERATURE) {
+    /* DomainTemperature2d::adjointCollideSource (domainTemperature2d.hh:28-38) */
+    double inv = (double)(1. / box_count(c->obj_out));
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          double* a = A + (((int64_t)z * m->ny + y) * m->nx + x) * Q;
+          for (int d = 0; d < 5; ++d) a[9 + d] += tc * inv;
+        }
+  } else if (c->objective == LBM_OBJ_REGENERATOR_EFFICIENCY) {
+    /* RegeneratorEfficiency2d::adjointCollideSource / adjointSensitivitySource
+     * (regeneratorEfficiency2d.hh:36-88) with timeConst where the derivative of
+     * the evaluate puts it: J_t = w N / D, N = sum (1-g)(T - Ti), D = sum (1-g)(Tb - Ti),
+     * dJ_t/dT = w (1-g)/D, dJ_t/dg = w ((Tb - Ti) N - (T - Ti) D) / D^2 (the
+     * reference divides by w D in the first and leaves w off the (T - Ti) D term in
+     * the second, which agree for w = 1 only). */
+    double Ti = c->obj_param[0], Tb = c->obj_param[1], vn = 0., vd = 0.;
+    const int* b = c->obj_out;
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          int64_t k = ((int64_t)z * m->ny + y) * m->nx + x;
+          const double* f = F + k * Q;
+          double T = f[9] + f[10] + f[11] + f[12] + f[13];
+          vn += (1. - gamma[k]) * (T - Ti);
+          vd += (1. - gamma[k]) * (Tb - Ti);
+        }
+    for (int z = b[4]; z <= b[5]; ++z)
+      for (int y = b[2]; y <= b[3]; ++y)
+        for (int x = b[0]; x <= b[1]; ++x) {
+          int64_t k = ((int64_t)z * m->ny + y) * m->nx + x;
+          double* a = A + k * Q;
+          const double* f = F + k * Q;
+          double T = f[9] + f[10] + f[11] + f[12] + f[13];
+          for (int d = 0; d < 5; ++d) a[9 + d] += tc * (1. - gamma[k]) / vd;
+          sens[k] += tc * ((Tb - Ti) * vn - (T - Ti) * vd) / (vd * vd);
         }
   } else if (c->objective == LBM_OBJ_HEAT_FLUX) {
     const int* b = c->obj_out;
@@ -1394,10 +1476,11 @@ static void adjoint_step(const model_t* m, const double* F, double* lam, double*
     memcpy(lam + k * Q, li, sizeof(double) * Q);
     sens[k] += dg;
   }
-  /* AdjointLBSolver::computeCollideSource (adjointLBSolver.cc:83-102) */
-  objective_source(m, F, gamma, lam, sens);
-  /* AdjointLBSolver::adjointStream (adjointLBSolver.cc:50-81) */
-  adjoint_bcs(m, t, lam);
+  /* AdjointLBSolver::computeCollideSource (adjointLBSolver.cc:83-102); none for the
+   * steps before the objective window (the regenerator's EmptyFunctional) */
+  if (t >= m->obj_from) objective_source(m, F, gamma, lam, sens);
+  /* AdjointLBSolver::adjointStream (adjointLBSolver.cc:50-81); f_0 has no boundary */
+  if (t >= 1) adjoint_bcs(m, t, lam);
   adjoint_stream_all(m, lam, tmp);
   copy_par(lam, tmp, m->ncell * m->Q);
 }
@@ -1458,10 +1541,9 @@ int orc_adjoint_step(const lbm_config* cfg, const double* gamma, const double* f
 
 /* Forward + reverse with a two-level store: every k-th state kept, the states
  * of one segment recomputed during the reverse sweep. */
-int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
-                 double* J_sum, double* sens) {
-  model_t m;
-  if (model_init(&m, cfg)) return -1;
+static int gradient_core(model_t* mp, const double* gamma, const double* macros, int nsteps,
+                         double* J_sum, double* sens) {
+  model_t m = *mp;
   int64_t S = m.ncell * m.Q;
   int k = (int)ceil(sqrt((double)nsteps + 1.));
   if (k < 1) k = 1;
@@ -1480,7 +1562,7 @@ int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macro
   for (int t = 0; t < nsteps; ++t) {
     if (t % k == 0) memcpy(ck + (int64_t)(t / k) * S, f, sizeof(double) * S);
     step(&m, f, tmp, gamma, t);
-    acc += objective(&m, f, gamma);
+    if (t + 1 >= m.obj_from) acc += objective(&m, f, gamma);
   }
   if (J_sum) *J_sum = acc;
   for (int64_t c = 0; c < m.ncell; ++c) sens[c] = 0.;
@@ -1507,6 +1589,56 @@ int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macro
   }
   free(ck); free(seg); free(f); free(tmp); free(lam);
   return 0;
+}
+
+int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
+                 double* J_sum, double* sens) {
+  model_t m;
+  if (model_init(&m, cfg)) return -1;
+  return gradient_core(&m, gamma, macros, nsteps, J_sum, sens);
+}
+
+/* The regenerator applications' gradient (applications/Regenerator2d/regenerator2d.cc:
+ * 266-387): a steady phase (the largest one-step change of any population, every
+ * check_every steps, below tol, or max_steady steps) without objective, then
+ * n_unsteady steps with it; the reverse sweep through both.  The steady phase is
+ * run once to find its length S and again inside the checkpointed sweep, with
+ * LBM_TIME_RAMP ramps starting at S. */
+int orc_gradient_steady(const lbm_config* cfg, const double* gamma, const double* macros,
+                        int max_steady, int check_every, double tol, int n_unsteady,
+                        double* J_sum, double* sens, int* steady_steps) {
+  model_t m;
+  if (model_init(&m, cfg)) return -1;
+  m.t_phase = 2147483647;
+  m.obj_from = 1;
+  int64_t S = m.ncell * m.Q;
+  double* f = (double*)malloc(sizeof(double) * S);
+  double* prev = (double*)malloc(sizeof(double) * S);
+  double* tmp = (double*)malloc(sizeof(double) * S);
+  if (!f || !prev || !tmp) {
+    free(f); free(prev); free(tmp);
+    return -4;
+  }
+  init_equilibrium(&m, macros, f);
+  int steps = 0;
+  while (steps < max_steady) {
+    memcpy(prev, f, sizeof(double) * S);
+    step(&m, f, tmp, gamma, steps);
+    ++steps;
+    if (steps % check_every == 0 || steps == max_steady) {
+      double mx = 0.;
+      for (int64_t i = 0; i < S; ++i) {
+        double d = fabs(f[i] - prev[i]);
+        if (d > mx || d != d) mx = d;
+      }
+      if (mx < tol) break;
+    }
+  }
+  free(f); free(prev); free(tmp);
+  if (steady_steps) *steady_steps = steps;
+  m.t_phase = steps;
+  m.obj_from = steps + 1;
+  return gradient_core(&m, gamma, macros, steps + n_unsteady, J_sum, sens);
 }
 
 int orc_macros(const lbm_config* cfg, const double* f, double* mac) {
@@ -1544,6 +1676,13 @@ int orc_reverse_cell(const lbm_config* cfg, const double* fin, double gamma, con
   double dg = 0.;
   cell_reverse(&m, fin, lo, lam_in, gamma, &dg);
   if (dgamma) *dgamma = dg;
+  return 0;
+}
+
+int orc_apply_bcs(const lbm_config* cfg, int t, double* f) {
+  model_t m;
+  if (model_init(&m, cfg)) return -1;
+  if (t >= 1) apply_bcs(&m, t, f);
   return 0;
 }
 

@@ -31,12 +31,22 @@ int orc_adjoint_step(const lbm_config* cfg, const double* gamma, const double* f
                      double* lam, double* sens);
 int orc_gradient(const lbm_config* cfg, const double* gamma, const double* macros, int nsteps,
                  double* J_sum, double* sens);
+/* Steady phase without objective, then n_unsteady steps with it; the reverse sweep
+ * through both (the library's lbm_gradient_steady). */
+int orc_gradient_steady(const lbm_config* cfg, const double* gamma, const double* macros,
+                        int max_steady, int check_every, double tol, int n_unsteady,
+                        double* J_sum, double* sens, int* steady_steps);
+/* Phase of the calls that follow: LBM_TIME_RAMP ramps start after step t_phase
+ * (2147483647 = never), the objective counts steps >= obj_from (default 1). */
+int orc_set_phase(int t_phase, int obj_from);
 int orc_macros(const lbm_config* cfg, const double* f, double* mac);
 int orc_collide_cell(const lbm_config* cfg, const double* fin, double gamma, double* fout,
                      double* mac);
 int orc_reverse_cell(const lbm_config* cfg, const double* fin, double gamma,
                      const double* lam_out, double* lam_in, double* dgamma);
 int orc_objective(const lbm_config* cfg, const double* f, const double* gamma, double* J);
+/* The boundary conditions of step t (t >= 1; none at t = 0) applied in place to f. */
+int orc_apply_bcs(const lbm_config* cfg, int t, double* f);
 int orc_wang_count(int nsteps, int nsnap, int64_t* recomputed, int* ok);
 int orc_static_count(int nsteps, int nsnap, int64_t* recomputed, int* ok, int* saved);
 /* Wall time of nsteps forward and nsteps reverse steps on nthreads threads (0 = all). */

@@ -51,6 +51,13 @@ def _bind(lib, prefix):
         lib.orc_macros.argtypes = [cp, _dp, _dp]
         lib.orc_objective.restype = C.c_int
         lib.orc_objective.argtypes = [cp, _dp, _dp, _dp]
+        lib.orc_apply_bcs.restype = C.c_int
+        lib.orc_apply_bcs.argtypes = [cp, C.c_int, _dp]
+        lib.orc_gradient_steady.restype = C.c_int
+        lib.orc_gradient_steady.argtypes = [cp, _dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int,
+                                            _dp, _dp, C.POINTER(C.c_int)]
+        lib.orc_set_phase.restype = C.c_int
+        lib.orc_set_phase.argtypes = [C.c_int, C.c_int]
     else:
         lib.ref_wang_count.restype = C.c_int
         lib.ref_wang_count.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_longlong),
@@ -142,6 +149,46 @@ class OracleLib:
         if rc:
             raise RuntimeError("reverse_cell failed: %d" % rc)
         return li, float(dg[0])
+
+    def objective(self, cfg: Config, f, gamma):
+        """weight * F of the populations f (FP64 AoS) as given (oracle only)."""
+        c = cfg.to_c()
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        J = C.c_double()
+        rc = self.lib.orc_objective(C.byref(c), _p(f), _p(g), C.byref(J))
+        if rc:
+            raise RuntimeError("objective failed: %d" % rc)
+        return J.value
+
+    def apply_bcs(self, cfg: Config, f, t):
+        """The boundary conditions of step t applied to a copy of f (oracle only)."""
+        c = cfg.to_c()
+        f = np.array(f, dtype=np.float64)
+        rc = self.lib.orc_apply_bcs(C.byref(c), int(t), _p(f))
+        if rc:
+            raise RuntimeError("apply_bcs failed: %d" % rc)
+        return f
+
+    def gradient_steady(self, cfg: Config, gamma, max_steady, check_every, tol, n_unsteady,
+                        macros=None):
+        """Steady phase, then n_unsteady objective steps; (J, dJ/dgamma, steady steps)."""
+        c = cfg.to_c()
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        s = np.zeros(cfg.ncells)
+        tot = np.zeros(1)
+        S = C.c_int()
+        m = None if macros is None else np.ascontiguousarray(macros, dtype=np.float64)
+        rc = self.lib.orc_gradient_steady(C.byref(c), _p(g), _p(m), int(max_steady),
+                                          int(check_every), float(tol), int(n_unsteady), _p(tot),
+                                          _p(s), C.byref(S))
+        if rc:
+            raise RuntimeError("gradient_steady failed: %d" % rc)
+        return float(tot[0]), s, S.value
+
+    def set_phase(self, t_phase=2147483647, obj_from=1):
+        """Ramps start after step t_phase; the objective counts steps >= obj_from."""
+        self.lib.orc_set_phase(int(t_phase), int(obj_from))
 
     def wang_count(self, nsteps, nsnap):
         if self.prefix == "orc_":
