@@ -17,6 +17,19 @@ LaunchFn launcher_d2q9(int collision, int storage) {
   return nullptr;
 }
 
+ChangeFn change_fn_d2q9(int collision, int storage) {
+  if (collision == LBM_BGK) {
+    if (storage == LBM_STORE_FP64) return &OpsImpl<LAT, LBM_BGK, double>::max_change;
+    if (storage == LBM_STORE_FP32) return &OpsImpl<LAT, LBM_BGK, float>::max_change;
+    if (storage == LBM_STORE_FP16) return &OpsImpl<LAT, LBM_BGK, __half>::max_change;
+  } else if (collision == LBM_MRT) {
+    if (storage == LBM_STORE_FP64) return &OpsImpl<LAT, LBM_MRT, double>::max_change;
+    if (storage == LBM_STORE_FP32) return &OpsImpl<LAT, LBM_MRT, float>::max_change;
+    if (storage == LBM_STORE_FP16) return &OpsImpl<LAT, LBM_MRT, __half>::max_change;
+  }
+  return nullptr;
+}
+
 BatchOps batch_ops_d2q9(int collision, int storage) {
   BatchOps o;
   if (collision == LBM_BGK && storage == LBM_STORE_FP64) {

@@ -147,6 +147,7 @@ struct lbm_handle {
   size_t adj_bytes = 0;  // bytes per adjoint value
   size_t gam_bytes = 0;  // bytes per design value
   LaunchFn launch = nullptr;
+  ChangeFn change = nullptr;   // max |f_t - f_{t-1}| of two states (steady runs)
   cudaStream_t stream = nullptr;
   Geometry geo;       // initialisation / export kernels
   Geometry geo_fwd;   // forward step (autotuned)
@@ -226,38 +227,6 @@ __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict_
     for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) tot += sh[w];
     *out = tot;
   }
-}
-
-// *bits = bit pattern of max |a - b| over the Q planes of ncell valid cells
-// (the padding at the end of each plane is skipped).  Non-negative doubles
-// order like their bit patterns, so an integer atomicMax finds the maximum in
-// any order; a NaN (positive pattern above every number) wins and is reported.
-template <class S>
-__global__ void k_max_change(const S* __restrict__ a, const S* __restrict__ b, int Q, long long P,
-                             long long ncell, unsigned long long* bits) {
-  double m = 0.;
-  const long long total = (long long)Q * ncell;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long q = i / ncell, c = i - q * ncell;
-    const double d = fabs((double)a[q * P + c] - (double)b[q * P + c]);
-    m = (d > m || d != d) ? d : m;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double v = __shfl_down_sync(0xffffffffu, m, o);
-    m = (v > m || v != v) ? v : m;
-  }
-  if ((threadIdx.x & 31) == 0) atomicMax(bits, (unsigned long long)__double_as_longlong(m));
-}
-
-void launch_max_change(size_t pop_bytes, const void* a, const void* b, int Q, long long P,
-                       long long ncell, unsigned long long* bits, unsigned blocks, cudaStream_t st) {
-  if (pop_bytes == 8)
-    k_max_change<double><<<blocks, 256, 0, st>>>((const double*)a, (const double*)b, Q, P, ncell, bits);
-  else if (pop_bytes == 4)
-    k_max_change<float><<<blocks, 256, 0, st>>>((const float*)a, (const float*)b, Q, P, ncell, bits);
-  else
-    k_max_change<__half><<<blocks, 256, 0, st>>>((const __half*)a, (const __half*)b, Q, P, ncell, bits);
 }
 
 // sens[c] += coef * (*J) over the cells of box b (x fastest): the design
@@ -658,6 +627,26 @@ int init_into(lbm_handle* h, void* out) {
 
 int init_state(lbm_handle* h) { return init_into(h, h->f[h->cur]); }
 
+// *out = max |f_t - f_{t-1}| over every population, the state `cur` of step
+// t_cur and `prev` of step t_cur - 1 each with its step's boundary conditions
+// (the reference's steady test compares post-boundary states).  bits: one
+// device word of scratch.  Waits for the result.
+int measure_change(lbm_handle* h, const void* cur, const void* prev, int t_cur,
+                   unsigned long long* bits, double* out) {
+  KParams pc = base_params(h, t_cur), pp = base_params(h, t_cur - 1);
+  pc.fin = cur;
+  pp.fin = prev;
+  CUDA_OR_FAIL(h, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), h->stream));
+  h->change(h->geo.grid, h->geo.block, h->stream, pc, pp, bits);
+  h->launches++;
+  CUDA_OR_FAIL(h, cudaGetLastError());
+  unsigned long long hb = 0;
+  CUDA_OR_FAIL(h, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OR_FAIL(h, cudaStreamSynchronize(h->stream));
+  memcpy(out, &hb, sizeof(double));
+  return 0;
+}
+
 // D = sum over obj_out of (1 - gamma)(Tb - Ti) of the regenerator efficiency,
 // from the design on the host.
 void set_regen_denominator(lbm_handle* h, const double* gamma) {
@@ -756,7 +745,10 @@ int lbm_create(const lbm_config* cfg, lbm_handle** out) {
   h->launch = c.lattice == LBM_D2Q9    ? launcher_d2q9(c.collision, c.storage)
               : c.lattice == LBM_D3Q19 ? launcher_d3q19(c.collision, c.storage)
                                        : launcher_thermal(c.collision, c.storage);
-  if (!h->launch) {
+  h->change = c.lattice == LBM_D2Q9    ? change_fn_d2q9(c.collision, c.storage)
+              : c.lattice == LBM_D3Q19 ? change_fn_d3q19(c.collision, c.storage)
+                                       : change_fn_thermal(c.collision, c.storage);
+  if (!h->launch || !h->change) {
     const int lat = c.lattice, coll = c.collision, stor = c.storage;   // c is h->cfg
     delete h;
     return fail(nullptr, LBM_ERR_SUP, "no kernel for lattice %d collision %d storage %d", lat, coll,
@@ -997,16 +989,7 @@ int lbm_forward_steady(lbm_handle* h, int max_steps, int check_every, double tol
     ++k;
     if (k % check_every == 0 || k == max_steps) {
       // the step's input is intact in the other state buffer
-      CUDA_OR_FAIL(h, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), h->stream));
-      const long long total = (long long)h->Q * h->ncell;
-      const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 4096);
-      launch_max_change(h->pop_bytes, h->f[h->cur], h->f[1 - h->cur], h->Q, h->P, h->ncell, bits,
-                        blocks, h->stream);
-      CUDA_OR_FAIL(h, cudaGetLastError());
-      unsigned long long hb = 0;
-      CUDA_OR_FAIL(h, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
-      CUDA_OR_FAIL(h, cudaStreamSynchronize(h->stream));
-      memcpy(&last, &hb, sizeof(last));
+      if ((rc = measure_change(h, h->f[h->cur], h->f[1 - h->cur], h->t, bits, &last))) return rc;
       if (!std::isfinite(last)) return fail(h, LBM_ERR_NONFINITE, "state is not finite at step %d", h->t);
       if (last < tol) break;
     }
@@ -1264,16 +1247,8 @@ int gradient_run(lbm_handle* h, int nsteps, int nsnap, int schedule, SteadyPhase
       if ((rc = save(place(steady)))) return rc;
       if (steady % sp->check_every == 0 || steady == sp->max_steps) {
         // the step's input is still intact in its buffer (the next step writes later)
-        CUDA_OR_FAIL(h, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), h->stream));
-        const long long total = (long long)h->Q * h->ncell;
-        const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 4096);
-        launch_max_change(h->pop_bytes, cur_buf(), pool_buffer(h, prev), h->Q, h->P, h->ncell,
-                          bits, blocks, h->stream);
-        CUDA_OR_FAIL(h, cudaGetLastError());
-        unsigned long long hb = 0;
-        CUDA_OR_FAIL(h, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, h->stream));
-        CUDA_OR_FAIL(h, cudaStreamSynchronize(h->stream));
-        memcpy(&sp->change, &hb, sizeof(double));
+        if ((rc = measure_change(h, cur_buf(), pool_buffer(h, prev), h->t, bits, &sp->change)))
+          return rc;
         if (!std::isfinite(sp->change))
           return fail(h, LBM_ERR_NONFINITE, "state is not finite at step %d", h->t);
         if (sp->change < sp->tol) break;

@@ -79,7 +79,9 @@ __device__ __forceinline__ bool interior(int x, int y, int z, const KParams& p) 
 // Boundary conditions live on the x = 0 and x = nx-1 faces and, in 2D, on
 // the y = 0 and y = ny-1 faces (checked when the handle is created; p.bc_y
 // says whether any does), so other cells skip the boundary loop.
+template <int LAT>
 __device__ __forceinline__ bool on_bc_face(int x, int y, const KParams& p) {
+  if (Lattice<LAT>::DIM == 3) return p.apply_bc && (x == 0 || x == p.nx - 1);
   return p.apply_bc && (x == 0 || x == p.nx - 1 || (p.bc_y && (y == 0 || y == p.ny - 1)));
 }
 
@@ -187,7 +189,7 @@ __device__ __forceinline__ typename Store<S>::C forward_cell_from(const KParams&
   C objv = C(0.);
   {
     S* __restrict__ fout = (S*)p.fout;
-    if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     if (p.eval_obj) objv = objective_cell<LAT, SHIFT>(f, g, x, y, z, p);
     const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     C rho, jx, jy, jz;
@@ -271,7 +273,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
   pull_all<LAT, A, C>(lam, lin, c, x, y, z, interior<LAT>(x, y, z, p), p);
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+  if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
   const C g = C(((const G*)p.gamma)[c]);
   const C imult = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
   const C dimult = C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q));
@@ -293,7 +295,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
       });
     }
     if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, d, dg, x, y, z, p);
-    if (on_bc_face(x, y, p)) {
+    if (on_bc_face<LAT>(x, y, p)) {
       static_for<L::Q>([&](auto Q_) {
         constexpr int q = decltype(Q_)::value;
         lam[q] += d[q];
@@ -337,7 +339,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
     });
   }
   if (p.eval_obj) objective_source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p);
-  if (on_bc_face(x, y, p)) adjoint_bcs<LAT>(lam, x, y, z, p);
+  if (on_bc_face<LAT>(x, y, p)) adjoint_bcs<LAT>(lam, x, y, z, p);
   static_for<L::Q>([&](auto Q_) {
     constexpr int q = decltype(Q_)::value;
     lout[q * (int)p.P + c] = A(lam[q]);
@@ -358,7 +360,7 @@ __device__ __forceinline__ typename Store<S>::C objective_only_cell(const KParam
     const int c = (z * p.ny + y) * p.nx + x;
     C f[L::Q];
     load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-    if (on_bc_face(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
+    if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
     v = objective_cell<LAT, SHIFT>(f, C(((const G*)p.gamma)[c]), x, y, z, p);
   }
   return v;
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(256) k_export(KParams p, double* __restrict__ 
   const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
   static_for<L::Q>([&](auto Q_) {
     constexpr int q = decltype(Q_)::value;
     aos[(long long)c * L::Q + q] = to_abs<LAT, S, q>(f[q]);
@@ -551,7 +553,7 @@ __global__ void __launch_bounds__(256) k_macros(KParams p, double* __restrict__ 
   const int c = (z * p.ny + y) * p.nx + x;
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-  if (on_bc_face(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
+  if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, p);
   C rho, jx, jy, jz;
   flow_macros<LAT>(f, rho, jx, jy, jz);
   double* m = mac + (long long)c * L::NMAC;
@@ -579,6 +581,40 @@ __global__ void __launch_bounds__(256) k_export_adjoint(KParams p, double* __res
     constexpr int q = decltype(Q_)::value;
     aos[(long long)c * L::Q + q] = lam[q];
   });
+}
+
+// *bits = bit pattern of max |f_t - f_{t-1}| over every population of every
+// cell, each state with its own step's boundary conditions applied on load
+// (the reference compares post-boundary states, regenerator2d.cc:160-170).
+// Non-negative doubles order like their bit patterns, so an integer atomicMax
+// finds the maximum in any order; a NaN (pattern above every number) wins.
+template <int LAT, class S>
+__global__ void __launch_bounds__(256) k_max_change_bc(const KParams pc, const KParams pp,
+                                                      unsigned long long* bits) {
+  using L = Lattice<LAT>;
+  using C = typename Store<S>::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double m = 0.;
+  if (x < pc.nx && y < pc.ny) {
+    const int c = (z * pc.ny + y) * pc.nx + x;
+    C f[L::Q], g[L::Q];
+    load_state<LAT, S>(f, (const S*)pc.fin, c, (int)pc.P);
+    load_state<LAT, S>(g, (const S*)pp.fin, c, (int)pp.P);
+    if (on_bc_face<LAT>(x, y, pc)) apply_bcs<LAT, Store<S>::SHIFT>(f, x, y, z, pc);
+    if (on_bc_face<LAT>(x, y, pp)) apply_bcs<LAT, Store<S>::SHIFT>(g, x, y, z, pp);
+    static_for<L::Q>([&](auto Q_) {
+      constexpr int q = decltype(Q_)::value;
+      const double d = fabs((double)f[q] - (double)g[q]);
+      m = (d > m || d != d) ? d : m;
+    });
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_down_sync(0xffffffffu, m, o);
+    m = (v > m || v != v) ? v : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(bits, (unsigned long long)__double_as_longlong(m));
 }
 
 template <class G>
@@ -640,6 +676,10 @@ struct OpsImpl {
       default:
         return nullptr;
     }
+  }
+  static void max_change(dim3 grid, dim3 block, cudaStream_t st, const KParams& cur,
+                         const KParams& prev, unsigned long long* bits) {
+    k_max_change_bc<LAT, S><<<grid, block, 0, st>>>(cur, prev, bits);
   }
   static void launch(int kind, dim3 grid, dim3 block, cudaStream_t st, const KParams& p,
                      double* aux) {

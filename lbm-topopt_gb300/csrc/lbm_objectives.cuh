@@ -373,21 +373,24 @@ __host__ __device__ constexpr ObjectiveInfo objective_info_at(ObjList<Os...>, in
   return all[k];
 }
 
+// The `||` fold stops at the objective that matches: the ones after it cost
+// no comparison (a `,` fold would test every entry at every cell).
 template <int LAT, bool SHIFT, class C, class... Os>
 __device__ __forceinline__ C objective_dispatch(ObjList<Os...>, const C* f, C g, int x, int y,
                                                 int z, const KParams& p) {
   C v = C(0.);
-  ((p.objective == Os::id ? (void)(v = Os::template evaluate<LAT, SHIFT>(f, g, x, y, z, p))
-                          : (void)0),
-   ...);
+  (void)((p.objective == Os::id &&
+          (v = Os::template evaluate<LAT, SHIFT>(f, g, x, y, z, p), true)) ||
+         ...);
   return v;
 }
 
 template <int LAT, bool SHIFT, class C, class... Os>
 __device__ __forceinline__ void source_dispatch(ObjList<Os...>, const C* f, C g, C* lam, C& dg,
                                                 int x, int y, int z, const KParams& p) {
-  ((p.objective == Os::id ? Os::template source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p) : (void)0),
-   ...);
+  (void)((p.objective == Os::id &&
+          (Os::template source<LAT, SHIFT>(f, g, lam, dg, x, y, z, p), true)) ||
+         ...);
 }
 
 // Weighted objective of one cell, in the compute precision.

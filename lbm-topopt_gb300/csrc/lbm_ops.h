@@ -30,6 +30,9 @@ typedef void (*LaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st, const
 
 typedef void (*BatchLaunchFn)(int kind, dim3 grid, dim3 block, cudaStream_t st,
                               const BatchParams& bp);
+// max |f_t - f_{t-1}| with each state's boundary conditions (k_max_change_bc)
+typedef void (*ChangeFn)(dim3 grid, dim3 block, cudaStream_t st, const KParams& cur,
+                         const KParams& prev, unsigned long long* bits);
 typedef const void* (*KernelAddressFn)(int kind);
 
 struct BatchOps {
@@ -44,6 +47,10 @@ BatchOps batch_ops_thermal(int collision, int storage);
 LaunchFn launcher_d2q9(int collision, int storage);
 LaunchFn launcher_d3q19(int collision, int storage);
 LaunchFn launcher_thermal(int collision, int storage);
+
+ChangeFn change_fn_d2q9(int collision, int storage);
+ChangeFn change_fn_d3q19(int collision, int storage);
+ChangeFn change_fn_thermal(int collision, int storage);
 
 // Text returned by lbm_last_error(NULL) (errors raised outside a handle).
 void set_global_error(const char* msg);

@@ -180,9 +180,13 @@ def test_noalloc_at_the_block_limit(nlib, orc):
     32768 D3Q19 lattice: blocks of 32 x 8 threads, one per z layer)."""
     pytest.importorskip("torch")
     cfg, gamma, _ = W.workload_duct_256x128x128(G.STORE_FP32, nx=3, ny=8, nz=32768, nsteps=1)
-    f0 = np.zeros(cfg.ncells * cfg.npop)
-    f0.reshape(cfg.ncells, 19)[:] = W3
-    f0 = f0 * (1 + 0.01 * np.sin(np.arange(f0.size)))
+    # uniform inflow: a parabolic one would need 6 x 32766 profile values
+    cfg.bcs[0] = G.Boundary(G.BC_VELOCITY, G.FACE_WEST, cfg.bcs[0].box, 0.04)
+    # a density falling along x (the pressure drop between the x = 0 and x = 2
+    # faces is then well conditioned), with some noise on top
+    x = np.arange(cfg.ncells) % cfg.nx
+    f0 = W3[None, :] * (1.0 + 0.01 * (2 - x)[:, None])
+    f0 = (f0 * (1 + 0.001 * np.sin(np.arange(f0.size)).reshape(f0.shape))).ravel()
     planes, held = _stored(cfg, f0)
     vals = _noalloc(nlib, cfg, 0, planes, gamma)
     ref = orc.objective(cfg.replace(storage=G.STORE_FP64), held,
