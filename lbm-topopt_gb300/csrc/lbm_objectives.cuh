@@ -266,21 +266,12 @@ struct ObjDissipation {
     const C alpha = C(0.5) * (mp<C>(p).pbb_scale * bp(g, mp<C>(p).pbb_q));
     const C tc = mp<C>(p).obj_weight;
     const C a4 = C(4.) * alpha, c2 = cv * C(2.), tr3 = tr / C(3.);
-    // dF/df_i = a4 (e.j) + c2 ((e.P e - tr/3) - 2 e.P j) is even in e through
-    // e.P e and odd through e.j and e.P j, so the opposite populations k and
-    // k + HALF take the even part E plus and minus the odd part O
-    const C tc2 = tc * c2, tc4 = tc * a4, m2tc2 = C(-2.) * tc2;
-    lam[0] += tc2 * (-tr3);
-    static_for<L::HALF>([&](auto D_) {
-      constexpr int k = decltype(D_)::value + 1;
-      static_assert(L::opp(k) == k + L::HALF, "pairs (k, k + HALF) are opposite");
-      const C ej = e_dot<LAT, k>(j[0], j[1], j[2]);
-      const C pej = e_dot<LAT, k>(pj[0], pj[1], pj[2]);   // e . P j
-      const C pe = e_quad<LAT, k>(P);                     // e . P e
-      const C E = tc2 * (pe - tr3);
-      const C O = tc4 * ej + m2tc2 * pej;
-      lam[k] += E + O;
-      lam[k + L::HALF] += E - O;
+    static_for<L::QF>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const C ej = e_dot<LAT, i>(j[0], j[1], j[2]);
+      const C pej = e_dot<LAT, i>(pj[0], pj[1], pj[2]);   // e . P j
+      const C pe = e_quad<LAT, i>(P);                     // e . P e
+      lam[i] += tc * (a4 * ej + c2 * ((pe - tr3) - C(2.) * pej));
     });
     C jj = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     dg += tc * (C(2.) * (C(0.5) * (mp<C>(p).pbb_scale * bp_diff(g, mp<C>(p).pbb_q))) * jj);
