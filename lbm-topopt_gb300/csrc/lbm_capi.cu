@@ -1627,12 +1627,16 @@ int batch_grid(lbm_batch* b, int kind, int total) {
 
 void batch_layout(lbm_batch* b, BatchParams& bp, int kind) {
   const dim3 blk = batch_block(b, kind);
+  // rows of cells per virtual block
+  const int rows = (int)blk.y * (kind == K_FORWARD                             ? kBatchRowsForward
+                                 : (kind == K_ADJOINT || kind == K_ADJOINT_LEAN) ? kBatchRowsReverse
+                                                                                 : 1);
   bp.n = b->n;
   int start = 0;
   for (int i = 0; i < b->n; ++i) {
     const lbm_handle* h = b->h[i];
     bp.gx[i] = (h->cfg.nx + (int)blk.x - 1) / (int)blk.x;
-    bp.gy[i] = (h->cfg.ny + (int)blk.y - 1) / (int)blk.y;
+    bp.gy[i] = (h->cfg.ny + rows - 1) / rows;
     // multiply-high divisors (batch_div): the numerators stay below the
     // lattice's block count gx*gy*nz (for gx) and gy*nz (for gy)
     const uint64_t nblk = (uint64_t)bp.gx[i] * bp.gy[i] * h->cfg.nz;
@@ -1651,6 +1655,7 @@ void batch_set_grids(lbm_batch* b) {
   BatchParams bp;
   batch_layout(b, bp, K_FORWARD);
   b->grid_fwd = batch_grid(b, K_FORWARD, bp.start[b->n]);
+  batch_layout(b, bp, K_OBJECTIVE);
   b->grid_obj = batch_grid(b, K_OBJECTIVE, bp.start[b->n]);
   batch_layout(b, bp, K_ADJOINT);
   b->grid_adj = batch_grid(b, b->adj_lean ? K_ADJOINT_LEAN : K_ADJOINT, bp.start[b->n]);

@@ -1958,6 +1958,12 @@ __device__ __forceinline__ void grid_reduce(C v, const KParams& p) {
 
 constexpr int kMaxBatch = LBM_MAX_BATCH;
 
+// Rows of cells (blockDim.y apart) each thread of a batched step kernel
+// advances: the lattice lookup and the parameter loads of a virtual block are
+// shared by them.  A virtual block covers blockDim.x x (blockDim.y * rows)
+// cells; the objective kernel keeps one row.
+constexpr int kBatchRowsForward = 2, kBatchRowsReverse = 1;
+
 struct BatchParams {
   int n;                        // lattices in the batch
   int start[kMaxBatch + 1];     // first virtual block of each lattice; start[n..kMaxBatch] = total

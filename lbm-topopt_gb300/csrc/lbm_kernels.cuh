@@ -430,8 +430,14 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
     const int bz = (int)batch_div((unsigned)r, (unsigned)bp.gy[i], bp.gym[i]);
     const int x = (lb - r * bp.gx[i]) * blockDim.x + threadIdx.x;
-    const int y = (r - bz * bp.gy[i]) * blockDim.y + threadIdx.y;
-    const auto objv = forward_cell<LAT, COLL, S>(p, x, y, bz);
+    const int y = (r - bz * bp.gy[i]) * (blockDim.y * kBatchRowsForward) + threadIdx.y;
+    // the rows' contributions summed in FP64, as the partial sums they join
+    // are: FP64 sums of FP32 values of similar size are exact, so the block
+    // shape does not change them
+    double objv = 0.;
+#pragma unroll 1
+    for (int k = 0; k < kBatchRowsForward; ++k)
+      objv += (double)forward_cell<LAT, COLL, S>(p, x, y + k * (int)blockDim.y, bz);
     if (p.eval_obj) grid_reduce_v(objv, p, lb, bp.start[i + 1] - bp.start[i]);
   }
 }
@@ -448,8 +454,10 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
     const int r = (int)batch_div((unsigned)lb, (unsigned)bp.gx[i], bp.gxm[i]);
     const int bz = (int)batch_div((unsigned)r, (unsigned)bp.gy[i], bp.gym[i]);
     const int x = (lb - r * bp.gx[i]) * blockDim.x + threadIdx.x;
-    const int y = (r - bz * bp.gy[i]) * blockDim.y + threadIdx.y;
-    adjoint_cell<LAT, COLL, S>(p, x, y, bz);
+    const int y = (r - bz * bp.gy[i]) * (blockDim.y * kBatchRowsReverse) + threadIdx.y;
+#pragma unroll 1
+    for (int k = 0; k < kBatchRowsReverse; ++k)
+      adjoint_cell<LAT, COLL, S>(p, x, y + k * (int)blockDim.y, bz);
   }
 }
 
