@@ -76,6 +76,38 @@ __device__ __forceinline__ bool interior(int x, int y, int z, const KParams& p) 
   return in;
 }
 
+// Whether every cell of the calling warp lies inside the lattice and one
+// cell away from every face; all 32 lanes must call it together (the step
+// kernels do so before any divergence).  With it (WARP below) the push and
+// the pull take the per-direction tests for the whole warp when one of its
+// cells needs them: the interior cells of a warp holding an x = 0 or
+// x = nx-1 cell would otherwise wait through both paths.  The same stores
+// either way.  The single-lattice 3D steps use it (256x128x128 duct, a
+// quarter of the warps hold a face cell: forward 0.1071 -> 0.1039 ms in
+// FP32, 0.0959 -> 0.0908 ms in FP16, reverse 0.1552 -> 0.1542 ms and 0.1487
+// -> 0.1471 ms); on the 2D lattices and in the batched steps, where few warps
+// hold a face cell, the vote cost more than it saved (batched forward step
+// 0.0342 -> 0.0352 ms, 4096x2048 D2Q9 reverse step 0.2178 -> 0.2197 ms), so
+// they test each lane where it pushes or pulls.
+template <int LAT>
+__device__ __forceinline__ bool warp_interior(int x, int y, int z, const KParams& p) {
+  return __all_sync(0xffffffffu, x < p.nx && y < p.ny && interior<LAT>(x, y, z, p));
+}
+
+// The interior decision of the push and the pull: the warp's (WARP) or the
+// cell's own.
+template <int LAT, bool WARP>
+__device__ __forceinline__ bool take_interior(bool warp_in, int x, int y, int z, const KParams& p) {
+  if constexpr (WARP)
+    return warp_in;
+  else
+    return interior<LAT>(x, y, z, p);
+}
+
+// Step kernels that decide the interior path per warp: the single-lattice 3D ones.
+template <int LAT>
+constexpr bool kWarpInterior = Lattice<LAT>::DIM == 3;
+
 // Boundary conditions live on the x = 0 and x = nx-1 faces and, in 2D, on
 // the y = 0 and y = ny-1 faces (checked when the handle is created; p.bc_y
 // says whether any does), so other cells skip the boundary loop.
@@ -178,11 +210,12 @@ __device__ __forceinline__ void pull_all(C* lam, const A* __restrict__ lin, int 
 
 // Forward step of cell (x,y,z) = index c from its loaded state f~_t (in f,
 // overwritten) and design value g; returns its objective contribution F(f_t).
-template <int LAT, int COLL, class S>
+// in: the warp's cells are all interior (warp_interior), read with WARP.
+template <int LAT, int COLL, class S, bool WARP>
 __device__ __forceinline__ typename Store<S>::C forward_cell_from(const KParams& p, int x, int y,
                                                                   int z, int c,
                                                                   typename Store<S>::C* f,
-                                                                  typename Store<S>::C g) {
+                                                                  typename Store<S>::C g, bool in) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   constexpr bool SHIFT = Store<S>::SHIFT;
@@ -212,22 +245,24 @@ __device__ __forceinline__ typename Store<S>::C forward_cell_from(const KParams&
           constexpr int q = decltype(I_)::value + 9;
           o[q] = Round<S>::apply(f[q], dq, rnd);
         });
-      push_all<LAT, S>(o, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
+      push_all<LAT, S>(o, fout, c, x, y, z, take_interior<LAT, WARP>(in, x, y, z, p), p);
     } else {
       flow_collide<LAT, COLL>(f, imult, rho, jx, jy, jz, p);
       if (LAT == LAT_D2Q9_D2Q5) {
         C T;
         thermal_collide(f + 9, jx, jy, g, T, p);
       }
-      push_all<LAT, S>(f, fout, c, x, y, z, interior<LAT>(x, y, z, p), p);
+      push_all<LAT, S>(f, fout, c, x, y, z, take_interior<LAT, WARP>(in, x, y, z, p), p);
     }
   }
   return objv;
 }
 
 // Forward step of cell (x,y,z); returns its objective contribution F(f_t).
-template <int LAT, int COLL, class S>
-__device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, int x, int y, int z) {
+// in: warp_interior of the calling warp, read with WARP.
+template <int LAT, int COLL, class S, bool WARP>
+__device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, int x, int y, int z,
+                                                             bool in) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
@@ -236,7 +271,7 @@ __device__ __forceinline__ typename Store<S>::C forward_cell(const KParams& p, i
     const int c = (z * p.ny + y) * p.nx + x;
     C f[L::Q];
     load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
-    objv = forward_cell_from<LAT, COLL, S>(p, x, y, z, c, f, C(((const G*)p.gamma)[c]));
+    objv = forward_cell_from<LAT, COLL, S, WARP>(p, x, y, z, c, f, C(((const G*)p.gamma)[c]), in);
   }
   return objv;
 }
@@ -257,9 +292,10 @@ __device__ __forceinline__ void add_sensitivity(double* sens, int c, double dg, 
     sens[c] += dg;
 }
 
-// Reverse step of cell (x,y,z).
-template <int LAT, int COLL, class S>
-__device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int z) {
+// Reverse step of cell (x,y,z); in: warp_interior of the calling warp, read
+// with WARP.
+template <int LAT, int COLL, class S, bool WARP>
+__device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int z, bool in) {
   using L = Lattice<LAT>;
   using C = typename Store<S>::C;
   using G = typename GammaT<S>::T;
@@ -270,7 +306,7 @@ __device__ __forceinline__ void adjoint_cell(const KParams& p, int x, int y, int
   const A* __restrict__ lin = (const A*)p.lam_in;
   A* __restrict__ lout = (A*)p.lam_out;
   C lam[L::Q];
-  pull_all<LAT, A, C>(lam, lin, c, x, y, z, interior<LAT>(x, y, z, p), p);
+  pull_all<LAT, A, C>(lam, lin, c, x, y, z, take_interior<LAT, WARP>(in, x, y, z, p), p);
   C f[L::Q];
   load_state<LAT, S>(f, (const S*)p.fin, c, (int)p.P);
   if (on_bc_face<LAT>(x, y, p)) apply_bcs<LAT, SHIFT>(f, x, y, z, p);
@@ -381,7 +417,9 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd) k_forward(K
   step_prologue();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const auto objv = forward_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
+  constexpr bool W = kWarpInterior<LAT>;
+  const bool in = W ? warp_interior<LAT>(x, y, blockIdx.z, p) : false;
+  const auto objv = forward_cell<LAT, COLL, S, W>(p, x, y, blockIdx.z, in);
   if (p.eval_obj) grid_reduce(objv, p);
 }
 
@@ -391,7 +429,9 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
   step_prologue();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  adjoint_cell<LAT, COLL, S>(p, x, y, blockIdx.z);
+  constexpr bool W = kWarpInterior<LAT>;
+  const bool in = W ? warp_interior<LAT>(x, y, blockIdx.z, p) : false;
+  adjoint_cell<LAT, COLL, S, W>(p, x, y, blockIdx.z, in);
 }
 
 // Objective of the state f_t alone (the last step of a forward sweep).
@@ -433,11 +473,14 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
     const int y = (r - bz * bp.gy[i]) * (blockDim.y * kBatchRowsForward) + threadIdx.y;
     // the rows' contributions summed in FP64, as the partial sums they join
     // are: FP64 sums of FP32 values of similar size are exact, so the block
-    // shape does not change them
+    // shape does not change them (and only where the objective is evaluated:
+    // GB300's FP64 pipe is narrow)
     double objv = 0.;
 #pragma unroll 1
-    for (int k = 0; k < kBatchRowsForward; ++k)
-      objv += (double)forward_cell<LAT, COLL, S>(p, x, y + k * (int)blockDim.y, bz);
+    for (int k = 0; k < kBatchRowsForward; ++k) {
+      const auto v = forward_cell<LAT, COLL, S, false>(p, x, y + k * (int)blockDim.y, bz, false);
+      if (p.eval_obj) objv += (double)v;
+    }
     if (p.eval_obj) grid_reduce_v(objv, p, lb, bp.start[i + 1] - bp.start[i]);
   }
 }
@@ -457,7 +500,7 @@ __global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
     const int y = (r - bz * bp.gy[i]) * (blockDim.y * kBatchRowsReverse) + threadIdx.y;
 #pragma unroll 1
     for (int k = 0; k < kBatchRowsReverse; ++k)
-      adjoint_cell<LAT, COLL, S>(p, x, y + k * (int)blockDim.y, bz);
+      adjoint_cell<LAT, COLL, S, false>(p, x, y + k * (int)blockDim.y, bz, false);
   }
 }
 
