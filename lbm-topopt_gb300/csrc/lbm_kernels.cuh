@@ -83,8 +83,8 @@ __device__ __forceinline__ bool interior(int x, int y, int z, const KParams& p) 
 // cells needs them: the interior cells of a warp holding an x = 0 or
 // x = nx-1 cell would otherwise wait through both paths.  The same stores
 // either way.  The single-lattice 3D steps use it (256x128x128 duct, a
-// quarter of the warps hold a face cell: forward 0.1071 -> 0.1039 ms in
-// FP32, 0.0959 -> 0.0908 ms in FP16, reverse 0.1552 -> 0.1542 ms and 0.1487
+// quarter of the warps hold a face cell: forward 0.1068 -> 0.1036 ms in
+// FP32, 0.0959 -> 0.0908 ms in FP16, reverse 0.1563 -> 0.1554 ms and 0.1487
 // -> 0.1471 ms); on the 2D lattices and in the batched steps, where few warps
 // hold a face cell, the vote cost more than it saved (batched forward step
 // 0.0342 -> 0.0352 ms, 4096x2048 D2Q9 reverse step 0.2178 -> 0.2197 ms), so
