@@ -33,13 +33,16 @@ struct Occupancy {
   static constexpr int adj = (LAT == LAT_D3Q19 && COLL == LBM_BGK) ? 3 : 4;
   // the register-lean reverse variant: one more resident block per SM (the
   // tuner picks it where the extra warps beat the spills, e.g. the D2Q9 BGK
-  // adjoint on lattices larger than L2)
+  // adjoint on lattices larger than L2); the batched D2Q9 one takes two more
+  // (6 blocks: the 8-channel batch's reverse step 0.0558 -> 0.0536 ms, while
+  // the 4096x2048 single-lattice step went 0.2000 -> 0.2145 ms with it)
   static constexpr int adj_lean = adj + 1;
+  static constexpr int adj_lean_batch = (LAT == LAT_D2Q9) ? adj + 2 : adj + 1;
   static constexpr bool has_lean = true;
 };
 template <int LAT, int COLL>
 struct Occupancy<LAT, COLL, double> {
-  static constexpr int fwd = 1, adj = 1, adj_lean = 1;
+  static constexpr int fwd = 1, adj = 1, adj_lean = 1, adj_lean_batch = 1;
   static constexpr bool has_lean = false;
 };
 
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(256, Occupancy<LAT, COLL, S>::fwd)
 }
 
 template <int LAT, int COLL, class S, bool LEAN = false>
-__global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean
+__global__ void __launch_bounds__(256, LEAN ? Occupancy<LAT, COLL, S>::adj_lean_batch
                                             : Occupancy<LAT, COLL, S>::adj)
     k_adjoint_batch(const __grid_constant__ BatchParams bp) {
   step_prologue();
