@@ -23,13 +23,15 @@ namespace lbm {
 // Resident 256-thread blocks per SM requested from the compiler (register
 // cap).  The FP32/FP16 step kernels are HBM-bound and need the warps to keep
 // enough loads in flight: 5 blocks (48 registers) measured fastest for the
-// D3Q19 MRT forward step and 4 (64 registers) for its adjoint; the D3Q19 BGK
-// adjoint in increment form needs more registers than 64 and gets 3 blocks
-// (85); the FP64 kernels are FP64-throughput-bound on GB300 and keep all
-// their registers.
+// D3Q19 MRT forward step and 4 (64 registers) for its adjoint; the D2Q9
+// forward step fits 6 (42 registers, no spills: 4096x2048 step 0.1079 ->
+// 0.1025 ms, the 8-channel batch's 0.0342 -> 0.0324 ms; 7 spills and is
+// slower); the D3Q19 BGK adjoint in increment form needs more registers than
+// 64 and gets 3 blocks (85); the FP64 kernels are FP64-throughput-bound on
+// GB300 and keep all their registers.
 template <int LAT, int COLL, class S>
 struct Occupancy {
-  static constexpr int fwd = 5;
+  static constexpr int fwd = (LAT == LAT_D2Q9) ? 6 : 5;
   static constexpr int adj = (LAT == LAT_D3Q19 && COLL == LBM_BGK) ? 3 : 4;
   // the register-lean reverse variant: one more resident block per SM (the
   // tuner picks it where the extra warps beat the spills, e.g. the D2Q9 BGK
