@@ -360,7 +360,7 @@ int lbm_get_launch_shape(const lbm_handle* h, int which, int* bx, int* by);
 
 /* Set the block shape of the forward (which = 0) or reverse (which = 1) step,
  * e.g. one found by lbm_autotune in an earlier run: bx a multiple of 32,
- * bx * by in {128, 256}.  No reference counterpart (the reference has no
+ * bx * by in {64, 128, 256}.  No reference counterpart (the reference has no
  * launch geometry). */
 int lbm_set_launch_shape(lbm_handle* h, int which, int bx, int by);
 
@@ -420,7 +420,8 @@ int lbm_batch_get_launch_shape(const lbm_batch* b, int* bx, int* by);
 int lbm_batch_get_reverse_shape(const lbm_batch* b, int* bx, int* by);
 /* Set the block shape of the batched forward and objective kernels
  * (which = 0) or of the batched reverse step (which = 1) to one of
- * lbm_batch_autotune's shapes (256x1, 128x2, 64x4, 32x8, 128x1, 64x2, 32x4),
+ * lbm_batch_autotune's shapes (256x1, 128x2, 64x4, 32x8, 128x1, 64x2, 32x4,
+ * 64x1, 32x2),
  * e.g. one it found in an earlier run.  No reference counterpart. */
 int lbm_batch_set_launch_shape(lbm_batch* b, int which, int bx, int by);
 /* Register variant of the batched reverse step (as lbm_set_reverse_variant). */

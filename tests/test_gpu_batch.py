@@ -73,9 +73,9 @@ def test_batch_d3q19_fp32_autotuned():
         for i, g in enumerate(gs):
             b[i].set_design(g)
         shape = b.autotune(2)
-        assert shape[0] * shape[1] in (128, 256)
+        assert shape[0] * shape[1] in (64, 128, 256)
         rshape = b.reverse_shape()
-        assert rshape[0] * rshape[1] in (128, 256) and rshape[0] % 32 == 0
+        assert rshape[0] * rshape[1] in (64, 128, 256) and rshape[0] % 32 == 0
         J, sens, _ = b.gradient(40, 5)
     for cfg, g, Jb, sb in zip(cfgs, gs, J, sens):
         with G.Handle(cfg) as h:

@@ -381,7 +381,7 @@ def test_launch_shape_does_not_change_results(storage):
     cfg = W.duct_3d(40, 12, 10, nsteps=30).replace(storage=storage)
     gamma = W.design_3d(40, 12, 10, 5)
     out = []
-    for shape in ((128, 2), (32, 4), (64, 2)):
+    for shape in ((128, 2), (32, 4), (64, 2), (64, 1), (32, 2)):
         with G.Handle(cfg) as h:
             h.set_launch_shape(0, *shape)
             h.set_launch_shape(1, *shape)
